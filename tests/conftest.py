@@ -1,0 +1,45 @@
+import os
+import sys
+import tempfile
+
+import numpy as np
+import pytest
+
+ROOT = os.path.abspath(os.path.join(os.path.dirname(__file__), ".."))
+if ROOT not in sys.path:
+    sys.path.insert(0, ROOT)
+
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+GOLDEN_CASES = sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
+
+
+def load_golden(name):
+    """(Problem, dict of reference dumps) for one committed fixture."""
+    from nbots_gb300 import problem_io as P
+    d = dict(np.load(os.path.join(GOLDEN, name + ".npz")))
+    pb = d.pop("problem_bin")
+    fd, path = tempfile.mkstemp(suffix=".bin")
+    with os.fdopen(fd, "wb") as f:
+        f.write(pb.tobytes())
+    try:
+        p = P.read_problem(path, name)
+    finally:
+        os.unlink(path)
+    return p, d
+
+
+@pytest.fixture(params=GOLDEN_CASES)
+def golden(request):
+    return (request.param,) + load_golden(request.param)
+
+
+def has_gpu():
+    try:
+        import torch
+        return torch.cuda.is_available()
+    except Exception:
+        return False
