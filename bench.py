@@ -1,0 +1,468 @@
+#!/usr/bin/env python
+"""Benchmark of the nbots FEM hot path on GB300.
+
+Workload (one GPU): 1024x512 Q4 plane-stress cantilever on [0,2]x[0,1],
+1,051,650 dof, per-element E = exp(N(0, 0.5^2)) (seed 2), nu = 0.3, left
+edge clamped, unit downward point load at the right-edge midpoint plus a
+uniform downward traction 0.01 on the top edge.  Synthetic, seeded inputs:
+nbots has no public benchmark set.
+
+A step is one solve of K u = F from u = 0 to ||F - K u|| <= 1e-8 ||F|| (true
+FP64 residual) with the mixed-precision Jacobi-PCG (FP32 inner iteration,
+FP64 reliable updates); the metric is the time per step.  Beside it the line
+carries the plain FP64 GPU CG, nbots' own FP64 iteration on the GPU, the SpMV
+bandwidths, the end-to-end time through the host-buffer C ABI, the roofline
+of the solver kernel and a CPU baseline.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+With --impl reference the oracle's C restatement of nbots' Jacobi-PCG runs on
+the host cores (OpenMP, all threads) on a bounded sample of iterations per
+step, projected to the iteration count nbots' algorithm needs on this
+workload.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 vs mixed-prec time-to-1e-8 relres at 1M DOF (s); SpMV HBM GB/s vs peak"
+WORKLOAD = ("C2: 1024x512 Q4 cantilever, 1,051,650 dof, lognormal E (sigma 0.5, seed 2), "
+            "clamped left edge, point load + top traction 0.01; Jacobi-PCG to relres 1e-8 from u=0")
+TOL = 1e-8
+# Jacobi-PCG iterations nbots' own algorithm (cg_precond_jacobi.c, FP64, one
+# thread) needs on this workload to reach ||g|| <= 1e-8 ||F||: measured by
+# running the oracle restatement to convergence (7017 on the GPU copy of the
+# same iteration).  Used to project the bounded CPU samples.
+NBOTS_ITERS_C2 = 7017
+CPU_SAMPLE_ITERS = 60
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as f:
+            d = json.load(f)
+        return float(d["hbm_gbs"]), "measured"
+    except Exception:
+        return 6800.0, "fallback"
+
+
+class Clocks:
+    """nvidia-smi samples during the timed region."""
+
+    def __init__(self, index=0):
+        self.index = index
+        self.rows = []
+        self.proc = None
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.index), "--query-gpu=clocks.sm,clocks.max.sm,"
+                 "power.draw,clocks_event_reasons.active,clocks_event_reasons.hw_slowdown,"
+                 "clocks_event_reasons.hw_thermal_slowdown,"
+                 "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.rows.append([c.strip() for c in line.split(",")])
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        sm = [float(r[0]) for r in self.rows if r and r[0].replace(".", "").isdigit()]
+        mx = [float(r[1]) for r in self.rows if len(r) > 1 and r[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[k] for r in self.rows for k in range(4)
+                          if len(r) > 4 + k and r[4 + k].lower() == "active"})
+        return {"sm_mhz": float(np.median(sm)) if sm else None,
+                "sm_max_mhz": max(mx) if mx else None, "reasons": reasons,
+                "samples": len(sm)}
+
+
+# ------------------------------------------------------------------ CPU
+def cpu_baseline(p, threads=None, iters=CPU_SAMPLE_ITERS):
+    """The oracle's restatement of nbots' Jacobi-PCG on the host cores: a
+    bounded run of `iters` iterations, projected to NBOTS_ITERS_C2."""
+    from oracle import oracle as O
+    threads = threads or os.cpu_count() or 1
+    fl = O.Flat(p)
+    rp, ci = O.pattern(fl)
+    _, K, F = O.assemble(fl, rp, ci)
+    O.set_bconditions(fl, rp, ci, K, F)
+    O.cg_jacobi(rp, ci, K, F, max_iter=2, tol=0.0, threads=threads)  # warm the threads
+    t0 = O.wtime()
+    O.cg_jacobi(rp, ci, K, F, max_iter=iters, tol=0.0, threads=threads)
+    dt = O.wtime() - t0
+    per_it = dt / iters
+    return {"value": per_it * NBOTS_ITERS_C2, "unit": "s", "cores": threads, "kind": "port",
+            "sample": f"{iters} Jacobi-PCG iterations of the C oracle (OpenMP, {threads} "
+                      f"threads) on the full workload, {per_it * 1e3:.2f} ms/iteration, "
+                      f"projected to {NBOTS_ITERS_C2} iterations"}
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    from nbots_gb300 import workloads as W
+    p = W.config_c2()
+    for _ in range(args.warmup):
+        cpu_baseline(p, iters=10)
+    vals = [cpu_baseline(p) for _ in range(args.steps)]
+    v = float(np.median([x["value"] for x in vals]))
+    cb = dict(vals[0])
+    cb["value"] = v
+    line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": WORKLOAD}, "impl": "reference", "cpu_baseline": cb,
+            "e2e": {"value": v, "unit": "s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+# ------------------------------------------------------------------ GPU
+def run_gpu(args):
+    import torch
+    import torch.distributed as dist
+    from nbots_gb300 import _lib as L
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.fem import FemSystem
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        dist.init_process_group("nccl")
+    torch.cuda.set_device(local)
+    lib = L.lib()
+    dev = torch.device("cuda", local)
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+
+    def barrier():
+        torch.cuda.synchronize()
+        if world > 1:
+            dist.barrier()
+
+    # ---- problem: assemble and apply BCs on the device (timed once)
+    p = W.config_c2()
+    t0 = time.perf_counter()
+    s = FemSystem(p, stream=sp)
+    t_create = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    assert s.assemble() == 0
+    s.apply_bcs()
+    A = s.block_layout()
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+    N, nnz = s.N, s.nnz
+    F = s.dptr(L.FEM_F)
+    u = torch.zeros(N, dtype=torch.float64, device=dev)
+    ws_bytes = max(lib.nbg_cg_mixed_workspace_bytes(N), lib.nbg_cg_bsr_workspace_bytes(N),
+                   lib.nbg_cg_workspace_bytes(N))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def mixed():
+        r = L.MixedResult()
+        rc = lib.nbg_cg_mixed(C.byref(A), F, u.data_ptr(), 4 * N, TOL, 0.1, L.CG_JACOBI |
+                              L.CG_RELATIVE, C.byref(r), ws.data_ptr(), ws_bytes, sp)
+        assert rc == 0 and r.status == 0, (rc, r.status, lib.nbg_last_error())
+        return r
+
+    def fp64():
+        r = L.CgResult()
+        rc = lib.nbg_cg_bsr_f64(C.byref(A), F, u.data_ptr(), 4 * N, TOL, L.CG_JACOBI |
+                                L.CG_RELATIVE, C.byref(r), ws.data_ptr(), ws_bytes, sp)
+        assert rc == 0 and r.status == 0, (rc, r.status)
+        return r
+
+    def timed(fn, steps, warmup, clocks=None):
+        for _ in range(warmup):
+            u.zero_()
+            fn()
+        times, res = [], None
+        barrier()
+        ctx = clocks if clocks is not None else _Null()
+        with ctx:
+            for _ in range(steps):
+                u.zero_()
+                flush.fill_(1.0)  # evict L2 (512 MB > 129 MB) between steps
+                e0 = torch.cuda.Event(enable_timing=True)
+                e1 = torch.cuda.Event(enable_timing=True)
+                e0.record(stream)
+                res = fn()
+                e1.record(stream)
+                e1.synchronize()
+                times.append(e0.elapsed_time(e1) / 1e3)
+        barrier()
+        return times, res
+
+    clk = Clocks(local)
+    t_mixed, r_mixed = timed(mixed, args.steps, args.warmup, clk)
+    u_mixed = u.clone()
+    t_fp64, r_fp64 = timed(fp64, max(1, min(args.steps, 3)), 1)
+    u_fp64 = u.clone()
+
+    # nbots' own iteration on the GPU (same absolute semantics, relative stop)
+    rp, ci, K = s.dptr(L.FEM_ROW_PTR), s.dptr(L.FEM_COL_IDX), s.dptr(L.FEM_K)
+
+    def nbots_gpu():
+        r = L.CgResult()
+        rc = lib.nbg_cg_f64(N, rp, ci, K, F, u.data_ptr(), 4 * N, TOL, L.CG_JACOBI |
+                            L.CG_RELATIVE, C.byref(r), ws.data_ptr(), ws_bytes, sp)
+        assert rc == 0, rc
+        return r
+    t_exact, r_exact = timed(nbots_gpu, 1, 0)
+
+    # ---- accuracy: true FP64 residuals and displacement differences
+    Ft = torch.from_numpy(s.get(L.FEM_F)).to(dev)
+
+    def relres(x):
+        y = torch.empty(N, dtype=torch.float64, device=dev)
+        lib.nbg_spmv_bsr_f64(C.byref(A), x.data_ptr(), y.data_ptr(), sp)
+        torch.cuda.synchronize()
+        return float(torch.linalg.norm(Ft - y) / torch.linalg.norm(Ft))
+    rr_mixed, rr_fp64 = relres(u_mixed), relres(u_fp64)
+    err_vs_fp64 = float(torch.linalg.norm(u_mixed - u_fp64) / torch.linalg.norm(u_fp64))
+
+    # ---- SpMV bandwidth (standalone kernels, L2 flushed before each launch)
+    def spmv_time(fn, n=20):
+        for _ in range(3):
+            fn()
+        ts = []
+        for _ in range(n):
+            flush.fill_(2.0)
+            e0 = torch.cuda.Event(enable_timing=True)
+            e1 = torch.cuda.Event(enable_timing=True)
+            e0.record(stream)
+            fn()
+            e1.record(stream)
+            e1.synchronize()
+            ts.append(e0.elapsed_time(e1) / 1e3)
+        return float(np.median(ts))
+    x64 = torch.randn(N, dtype=torch.float64, device=dev)
+    y64 = torch.empty_like(x64)
+    x32 = x64.float()
+    y32 = torch.empty_like(x32)
+    ent = A.n_entries
+    nblk = nnz // 4
+    t_csr = spmv_time(lambda: lib.nbg_spmv_csr_f64(N, rp, ci, K, x64.data_ptr(), y64.data_ptr(), sp))
+    t_b64 = spmv_time(lambda: lib.nbg_spmv_bsr_f64(C.byref(A), x64.data_ptr(), y64.data_ptr(), sp))
+    t_b32 = spmv_time(lambda: lib.nbg_spmv_bsr_f32(C.byref(A), x32.data_ptr(), y32.data_ptr(), sp))
+    hbm, peak_kind = peaks()
+    B_csr = 12 * nnz + 4 * (N + 1) + 8 * N + 8 * N
+    B_b64 = 36 * nblk + 4 * (A.n_slices + 1) + 16 * N
+    B_b32 = 20 * nblk + 4 * (A.n_slices + 1) + 8 * N
+    spmv = {"fp64_csr_nbots_order": {"us": t_csr * 1e6, "gbs": B_csr / t_csr / 1e9,
+                                     "frac": B_csr / t_csr / 1e9 / hbm, "bytes": B_csr},
+            "fp64_block": {"us": t_b64 * 1e6, "gbs": B_b64 / t_b64 / 1e9,
+                           "frac": B_b64 / t_b64 / 1e9 / hbm, "bytes": B_b64},
+            "fp32_block": {"us": t_b32 * 1e6, "gbs": B_b32 / t_b32 / 1e9,
+                           "frac": B_b32 / t_b32 / 1e9 / hbm, "bytes": B_b32},
+            "peak_gbs": hbm, "peak_kind": peak_kind, "l2": "flushed before each launch"}
+
+    # ---- roofline of the mixed solver kernel: algorithmic bytes per iteration
+    # matrix: FP32 hi (16 B) + bf16 lo (8 B) + column (4 B) per 2x2 block;
+    # vectors: L1 12 B/dof, L2 40 B/dof, L3 20 B/dof (72 B/dof).
+    it = r_mixed.niter
+    t_med = float(np.median(t_mixed))
+    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 72 * N
+    upd_bytes = r_mixed.n_updates * (36 * nblk + 8 * N * 5)
+    achieved = (bytes_iter * it + upd_bytes) / t_med / 1e9
+    traffic = None
+    tpath = os.path.join(ROOT, "profiles", "mixed_cg_traffic.json")
+    if os.path.exists(tpath):
+        with open(tpath) as f:
+            traffic = json.load(f).get("dram_bytes_per_iteration")
+
+    # ---- end to end through the host-buffer C ABI (pinned host memory)
+    rp_h, ci_h, K_h, F_h = (s.get(L.FEM_ROW_PTR), s.get(L.FEM_COL_IDX), s.get(L.FEM_K),
+                            s.get(L.FEM_F))
+    pin = []
+
+    def pinned(a):
+        ptr = C.c_void_p()
+        L.check(lib.nbg_host_alloc(C.byref(ptr), a.nbytes), "host_alloc")
+        pin.append(ptr)
+        b = np.ctypeslib.as_array((C.c_uint8 * a.nbytes).from_address(ptr.value)).view(a.dtype)
+        b[:] = a
+        return b
+    Kp, Fp, xp = pinned(K_h), pinned(F_h), pinned(np.zeros(N))
+    solver = C.c_void_p()
+    L.check(lib.nbg_solver_create(C.byref(solver), sp), "solver_create")
+    L.check(lib.nbg_solver_set_matrix(solver, N, rp_h.ctypes.data, ci_h.ctypes.data,
+                                      Kp.ctypes.data, 0), "set_matrix")
+    info = L.SolveInfo()
+
+    def e2e_step():
+        xp[:] = 0.0
+        L.check(lib.nbg_solver_set_matrix(solver, N, rp_h.ctypes.data, ci_h.ctypes.data,
+                                          Kp.ctypes.data, L.PATTERN_SAME), "set_matrix")
+        rc = lib.nbg_solver_solve(solver, Fp.ctypes.data, xp.ctypes.data, 4 * N, TOL,
+                                  L.CG_JACOBI | L.CG_RELATIVE, L.METHOD_MIXED, C.byref(info))
+        assert rc == 0, rc
+    for _ in range(max(1, args.warmup)):
+        e2e_step()
+    e2e_t = []
+    for _ in range(args.steps):
+        flush.fill_(3.0)
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        e2e_t.append(time.perf_counter() - t0)
+    lib.nbg_solver_destroy(solver)
+    e2e_v = float(np.median(e2e_t))
+    for ptr in pin:
+        lib.nbg_host_free(ptr)
+
+    # ---- max over ranks
+    vals = torch.tensor([t_med, e2e_v], dtype=torch.float64, device=dev)
+    if world > 1:
+        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
+    t_all, e2e_all = float(vals[0]), float(vals[1])
+
+    cpu = None
+    if rank == 0 and not args.no_cpu_baseline:
+        cpu = cpu_baseline(p)
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": t_all, "unit": "s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3,
+            "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32 inner (FP32+bf16 split operands) / f64 residual", "data": "synthetic",
+            "config": {"workload": WORKLOAD, "dof": N, "nnz": nnz, "tol": TOL,
+                       "l2": "flushed (512 MB write) before every timed solve",
+                       "replicas": world},
+            "mixed": {"s_per_solve": t_all, "iters": it, "updates": r_mixed.n_updates,
+                      "relres_fp64": rr_mixed, "us_per_iter": t_med / max(it, 1) * 1e6,
+                      "err_vs_fp64_rel_l2": err_vs_fp64},
+            "fp64_gpu": {"s_per_solve": float(np.median(t_fp64)), "iters": r_fp64.niter,
+                         "relres_fp64": rr_fp64,
+                         "us_per_iter": float(np.median(t_fp64)) / max(r_fp64.niter, 1) * 1e6},
+            "nbots_order_fp64_gpu": {"s_per_solve": float(t_exact[0]), "iters": r_exact.niter},
+            "speedup_mixed_vs_fp64_gpu": float(np.median(t_fp64)) / t_all,
+            "setup_s": {"pattern_and_upload": t_create, "assembly_and_bcs": t_asm},
+            "spmv": spmv,
+            "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
+                         "frac": achieved / hbm, "peak_kind": peak_kind,
+                         "traffic": traffic, "kernel": "k_cg_mixed",
+                         "bytes_per_iter": bytes_iter},
+            "e2e": {"value": e2e_all, "unit": "s",
+                    "h2d_bytes_per_step": int(8 * nnz + 16 * N),
+                    "d2h_bytes_per_step": int(8 * N),
+                    "path": "nbg_solver_set_matrix (values, pattern kept) + nbg_solver_solve "
+                            "(mixed) from pinned host buffers"},
+            "cpu_baseline": cpu,
+            "gpu_launches": args.steps,
+            "clocks": clk.summary(),
+        }
+        print(json.dumps(line))
+    if world > 1:
+        dist.destroy_process_group()
+    s.close()
+    return 0
+
+
+def run_profile(args):
+    """One bounded launch of a solver kernel on the full workload, for ncu:
+    `iters` iterations with a tolerance that is never met and reliable
+    updates only at the end, so DRAM bytes / iters is the per-iteration
+    traffic."""
+    import torch
+    from nbots_gb300 import _lib as L
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.fem import FemSystem
+    lib = L.lib()
+    p = W.config_c2()
+    s = FemSystem(p)
+    assert s.assemble() == 0
+    s.apply_bcs()
+    A = s.block_layout()
+    N = s.N
+    F = s.dptr(L.FEM_F)
+    u = torch.zeros(N, dtype=torch.float64, device="cuda")
+    ws_bytes = max(lib.nbg_cg_mixed_workspace_bytes(N), lib.nbg_cg_bsr_workspace_bytes(N))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
+    x64 = torch.randn(N, dtype=torch.float64, device="cuda")
+    y64 = torch.empty_like(x64)
+    x32, y32 = x64.float(), torch.empty(N, dtype=torch.float32, device="cuda")
+    for _ in range(2):
+        u.zero_()
+        if args.profile == "mixed":
+            r = L.MixedResult()
+            lib.nbg_cg_mixed(C.byref(A), F, u.data_ptr(), args.iters, 1e-30, 1e-12,
+                             L.CG_JACOBI | L.CG_RELATIVE, C.byref(r), ws.data_ptr(), ws_bytes,
+                             None)
+        elif args.profile == "fp64":
+            r = L.CgResult()
+            lib.nbg_cg_bsr_f64(C.byref(A), F, u.data_ptr(), args.iters, 1e-30,
+                               L.CG_JACOBI | L.CG_RELATIVE, C.byref(r), ws.data_ptr(), ws_bytes,
+                               None)
+        else:
+            for _ in range(3):
+                lib.nbg_spmv_bsr_f64(C.byref(A), x64.data_ptr(), y64.data_ptr(), None)
+                lib.nbg_spmv_bsr_f32(C.byref(A), x32.data_ptr(), y32.data_ptr(), None)
+                lib.nbg_spmv_csr_f64(N, s.dptr(L.FEM_ROW_PTR), s.dptr(L.FEM_COL_IDX),
+                                     s.dptr(L.FEM_K), x64.data_ptr(), y64.data_ptr(), None)
+        torch.cuda.synchronize()
+    print(json.dumps({"profile": args.profile, "iters": args.iters, "dof": N,
+                      "block_entries": int(A.n_entries), "blocks": s.nnz // 4}))
+    s.close()
+    return 0
+
+
+class _Null:
+    def __enter__(self):
+        return self
+
+    def __exit__(self, *a):
+        return False
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=5)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--profile", choices=["mixed", "fp64", "spmv"],
+                    help="one bounded kernel launch for ncu instead of the benchmark")
+    ap.add_argument("--iters", type=int, default=100)
+    args = ap.parse_args()
+    if args.profile:
+        return run_profile(args)
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gpu(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

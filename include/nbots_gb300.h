@@ -1,0 +1,308 @@
+/*
+ * nbots_gb300: thin C ABI over the sm_103a CUDA kernels of nbots' 2D
+ * linear-elastic FEM hot path.
+ *
+ * Two layers share this header:
+ *   - device-pointer kernels (nbg_*): every array argument is a device
+ *     pointer, `stream` is a cudaStream_t (NULL = legacy default stream),
+ *     and scratch memory comes either from the caller (ws, ws_bytes) or,
+ *     when ws is NULL, from cudaMalloc inside the call;
+ *   - host-buffer conveniences (nbg_host_*, nbg_fem_*) used by the C
+ *     drop-in of nbots' own entry points (include/nbots_dropin.h).
+ *
+ * Status codes: 0 success; positive values keep nbots' meanings (1 = CG did
+ * not reach the tolerance, cg_precond_jacobi.c:86-89; 1 = distorted
+ * element, static_elasticity2D.c:62-66); negative values are errors that
+ * nbots has no code for.  No entry point exits the process or traps the GPU.
+ */
+#ifndef NBOTS_GB300_H
+#define NBOTS_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define NBG_OK 0
+#define NBG_NOT_CONVERGED 1
+#define NBG_DISTORTED 1
+#define NBG_ERR_CUDA (-1)
+#define NBG_ERR_TIMEOUT (-2)     /* a device-side wait ran out its limit */
+#define NBG_ERR_ARG (-3)
+#define NBG_ERR_NOMEM (-4)
+#define NBG_ERR_PATTERN (-5)     /* an element pair is missing from the CSR pattern */
+#define NBG_ERR_BREAKDOWN (-6)   /* CG met a zero or non-finite curvature */
+
+/* ------------------------------------------------------------------ misc */
+const char *nbg_version(void);
+int nbg_device_count(void);
+/* Last CUDA error text seen by the library in this thread. */
+const char *nbg_last_error(void);
+
+int nbg_dev_alloc(void **ptr, size_t bytes);
+int nbg_dev_free(void *ptr);
+int nbg_h2d(void *dst, const void *src, size_t bytes, void *stream);
+int nbg_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int nbg_stream_sync(void *stream);
+
+/* -------------------------------------------------------------- assembly */
+/* Element stiffness and load of every element in nbots' operation order
+ * (replaces the per-element work of pipeline_assemble_system,
+ * pde_bot/finite_element/solid_mechanics/pipeline.c:83-230).
+ * nen = 3 (T3) or 4 (Q4).  Ke: N_elem x (2nen)^2 row-major; Fe: N_elem x 2nen.
+ * E: one modulus per element.  enabled may be NULL (all enabled).
+ * distorted: one device uint32, set to the smallest distorted element id
+ * (detJ < 0, utils.c:44-47) or left untouched; initialise it to UINT32_MAX. */
+int nbg_element_stiffness_f64(uint32_t nen, uint32_t N_elem, const double *nod,
+                              const uint32_t *conn, const double *E, double nu,
+                              double thickness, double density, int self_weight,
+                              double gx, double gy, const uint8_t *enabled,
+                              double *Ke, double *Fe, uint32_t *distorted,
+                              void *stream);
+
+/* Row-gather assembly into the CSR of nb_sparse_create(graph, NULL, 2)
+ * (sparse.c:20-60) in ascending element order, so K and F equal nbots'
+ * serial scatter (pipeline.c:60-69, 232-264) bit for bit; no float atomics.
+ * inc_ptr/inc_elem/inc_local: node -> (element, local node) incidence sorted
+ * by element id.  matched: one device uint64 counter, incremented by the
+ * number of (node block, shared element) pairs found; it ends at
+ * N_elem * nen^2 exactly when every element node pair is in the pattern
+ * (nbots exits on a missing pair, sparse.c:213-218). */
+int nbg_gather_assemble_f64(uint32_t nen, uint32_t N_nod, uint32_t N_elem,
+                            const uint32_t *inc_ptr, const uint32_t *inc_elem,
+                            const uint8_t *inc_local, const uint32_t *row_ptr,
+                            const uint32_t *col_idx, const double *Ke, const double *Fe,
+                            double *K, double *F, unsigned long long *matched, void *stream);
+
+/* Sequential load increments F[idx[k]] += inc[k], in k order per index
+ * (the Neumann loops of set_bconditions.c:63-190), grouped by index:
+ * group g adds inc[group_ptr[g] .. group_ptr[g+1]) to F[idx_of_group[g]]
+ * in that order. */
+int nbg_apply_increments_f64(uint32_t n_groups, const uint32_t *idx_of_group,
+                             const uint32_t *group_ptr, const double *inc,
+                             double *F, void *stream);
+
+/* Dirichlet elimination in nbots' event order (nb_sparse_set_Dirichlet_condition,
+ * sparse.c:416-430, called per masked dof in set_bconditions.c:192-260).
+ * Events are (dof, value) in application order; ev_ptr (N+1) lists, per
+ * dof, the event numbers that touch it in ascending order (ev_of). */
+int nbg_dirichlet_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+                      double *K, double *F, const uint32_t *ev_ptr, const uint32_t *ev_of,
+                      const double *ev_val, int *status, void *stream);
+
+/* Strain at Gauss points (pipeline.c:266-319) and stress from strain with
+ * one modulus per element (static_elasticity2D.c:99-127). */
+int nbg_strain_f64(uint32_t nen, uint32_t N_elem, const double *nod, const uint32_t *conn,
+                   const double *u, double *strain, void *stream);
+int nbg_stress_f64(uint32_t nen, uint32_t N_elem, const double *E, double nu,
+                   const uint8_t *enabled, const double *strain, double *stress,
+                   void *stream);
+
+/* ------------------------------------------------------------------ SpMV */
+/* y = A x with nbots' per-row left-to-right sum and no FMA
+ * (nb_sparse_multiply_vector, sparse.c:405-414): bit-exact. */
+int nbg_spmv_csr_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+                     const double *val, const double *x, double *y, void *stream);
+
+/* --------------------------------------------------------------------- CG */
+#define NBG_CG_JACOBI 1u     /* Jacobi preconditioner (else plain CG) */
+#define NBG_CG_RELATIVE 2u   /* stop on ||g|| <= tol ||b|| (else absolute, nbots) */
+
+typedef struct {
+    uint32_t niter;       /* iterations performed */
+    int status;           /* 0, 1 = not converged, < 0 error */
+    double tol_reached;   /* nbots' lagged sqrt(dot_gg) */
+    double bnorm;         /* ||b||_2 */
+} nbg_cg_result_t;
+
+/* Persistent FP64 CG in one cooperative launch, nbots' iteration
+ * (cg_precond_jacobi.c:13-90 with NBG_CG_JACOBI, conjugate_gradient.c:13-77
+ * without): g = Ax - b, lagged convergence test, division by the diagonal.
+ * x holds x0 on entry.  Reductions are fixed-order (run-to-run identical). */
+size_t nbg_cg_workspace_bytes(uint32_t N);
+int nbg_cg_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+               const double *val, const double *b, double *x, uint32_t max_iter,
+               double tol, unsigned flags, nbg_cg_result_t *result, void *ws,
+               size_t ws_bytes, void *stream);
+
+/* ------------------------------------------------- 2x2-block SELL layout */
+/* Device arrays of the node-block layout of a CSR from nb_sparse_create(.., 2)
+ * (two rows per node with the same (2w, 2w+1) column pairs, sparse.c:36-52):
+ * entry (slice s, k, lane r) sits at (slice_off[s] + k) * 32 + r; b64 holds
+ * 4 doubles (a00 a01 a10 a11) per entry, b32 the same rounded to float and
+ * blo the bfloat16 rounding of the remainders (double - float), so that
+ * b32 + blo carries about 32 significant bits; dinv = 1 / diagonal per
+ * scalar row.  Any array may be NULL when a caller does not need it. */
+typedef struct {
+    uint32_t N;            /* scalar rows (= 2 Nn) */
+    uint32_t Nn;           /* node rows */
+    uint32_t n_slices;     /* ceil(Nn / 32) */
+    uint64_t n_entries;    /* 32 * slice_off[n_slices] */
+    const uint32_t *slice_off;
+    const uint32_t *bcol;
+    const double *b64;
+    const float *b32;
+    const uint16_t *blo;   /* 4 bfloat16 per entry */
+    const double *dinv64;
+    const float *dinv32;
+} nbg_bsr_t;
+
+/* Host: check the block structure of a CSR and write the slice offsets
+ * (n_slices + 1 entries).  NBG_ERR_PATTERN if it is not node-blocked. */
+int nbg_bsr_plan(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+                 uint32_t *slice_off);
+/* Device: fill bcol/b64/b32/dinv from the CSR (device pointers). */
+int nbg_bsr_fill(const nbg_bsr_t *A, const uint32_t *row_ptr, const uint32_t *col_idx,
+                 const double *val, void *stream);
+int nbg_spmv_bsr_f64(const nbg_bsr_t *A, const double *x, double *y, void *stream);
+int nbg_spmv_bsr_f32(const nbg_bsr_t *A, const float *x, float *y, void *stream);
+
+/* Fast persistent FP64 Jacobi-PCG on the block layout: FMA arithmetic,
+ * reciprocal diagonal, stop on the current ||g|| (not nbots' lagged one);
+ * NBG_CG_RELATIVE selects ||g|| <= tol ||b||.  x holds x0 on entry. */
+size_t nbg_cg_bsr_workspace_bytes(uint32_t N);
+int nbg_cg_bsr_f64(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_iter,
+                   double tol, unsigned flags, nbg_cg_result_t *result, void *ws,
+                   size_t ws_bytes, void *stream);
+
+/* Mixed-precision Jacobi-PCG with reliable updates.  The Krylov iteration
+ * runs entirely on the FP32 pipes: matrix b32 + blo, residual in FP32,
+ * search direction and A p as FP32 + bfloat16 pairs, the correction as an
+ * FP32 pair, products and sums by error-free transformations (TwoProd /
+ * TwoSum) and dot products with Kahan-compensated FP32 sums.  Whenever the
+ * FP32 residual has dropped by `delta` since the last update (and at the
+ * end) the correction is added to the FP64 solution x and the residual is
+ * recomputed in FP64 as r = b - A x on b64.  Convergence is judged on that
+ * FP64 residual. */
+typedef struct {
+    uint32_t niter;        /* FP32 iterations */
+    uint32_t n_updates;    /* FP64 residual recomputations */
+    int status;            /* 0 converged, 1 not converged, < 0 error */
+    double relres;         /* final FP64 ||b - A x|| / ||b|| */
+    double bnorm;
+} nbg_mixed_result_t;
+
+size_t nbg_cg_mixed_workspace_bytes(uint32_t N);
+int nbg_cg_mixed(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_iter,
+                 double tol, double delta, unsigned flags, nbg_mixed_result_t *result,
+                 void *ws, size_t ws_bytes, void *stream);
+
+/* ------------------------------------------------- host-buffer solver */
+/* A CSR system in host memory (nb_sparse_create layout) solved on the GPU.
+ * Device buffers persist in the context between calls; with
+ * NBG_PATTERN_SAME a call re-sends only the values. */
+#define NBG_METHOD_NBOTS 0   /* nbots' iteration in FP64 (nbg_cg_f64) */
+#define NBG_METHOD_FP64 1    /* fast FP64 on the block layout (nbg_cg_bsr_f64) */
+#define NBG_METHOD_MIXED 2   /* mixed precision, FP64 reliable updates (nbg_cg_mixed) */
+#define NBG_PATTERN_SAME 1u
+
+typedef struct {
+    uint32_t niter;
+    uint32_t n_updates;    /* mixed precision: FP64 residual recomputations */
+    int status;
+    double relres;         /* final ||r|| / ||b|| the solver judged */
+    double tol_reached;    /* final ||r|| */
+} nbg_solve_info_t;
+
+typedef struct nbg_solver nbg_solver_t;
+int nbg_solver_create(nbg_solver_t **out, void *stream);
+void nbg_solver_destroy(nbg_solver_t *s);
+int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
+                          const uint32_t *col_idx, const double *val, unsigned flags);
+/* x holds x0 on entry and the solution on return (host memory). */
+int nbg_solver_solve(nbg_solver_t *s, const double *b, double *x, uint32_t max_iter,
+                     double tol, unsigned flags, int method, nbg_solve_info_t *info);
+
+/* Page-locked host memory (for asynchronous copies). */
+int nbg_host_alloc(void **ptr, size_t bytes);
+int nbg_host_free(void *ptr);
+
+/* ============================================================ host layer */
+/* Mesh arrays on the host, nbots' layout (mshquad_struct.h:6-26,
+ * msh3trg_struct.h:6-23): coordinates nod[2 i], connectivity conn[e nen + k]
+ * counter-clockwise, edges edg[2 i]. */
+typedef struct {
+    uint32_t nen, N_nod, N_elem, N_edg;
+    const double *nod;
+    const uint32_t *conn;
+    const uint32_t *edg;
+} nbg_mesh_t;
+
+/* One nbots bc atom (bc_atom.h:7-12, pushed by nb_bcond_push / _function):
+ * kind 0 Dirichlet / 1 Neumann; where 0 input vertex / 1 input segment.
+ * A function-valued atom carries its values where nbots evaluates them:
+ * one row per segment node, or one row for a vertex (Neumann vertex loads
+ * are read at (0,0), set_bconditions.c:156-171). */
+typedef struct {
+    uint32_t kind, where, id;
+    uint8_t mask[2];
+    double val[2];
+    uint32_t n_nv;
+    const double *node_vals;
+} nbg_bc_t;
+
+typedef struct {
+    const uint32_t *vtx;        /* input vertex -> node */
+    uint32_t N_sgm;
+    const uint32_t *sgm_ptr;    /* N_sgm + 1 offsets into sgm_nodes */
+    const uint32_t *sgm_nodes;  /* node sequence of each input segment */
+    uint32_t N_bc;
+    const nbg_bc_t *bc;         /* push order */
+} nbg_bcs_t;
+
+/* CSR pattern of nb_sparse_create(nodal graph, NULL, 2) (load_graph.c:230-328,
+ * sparse.c:20-60).  row_ptr has 2 N_nod + 1 entries; with col_idx NULL only
+ * row_ptr is filled (its last entry is nnz). */
+int nbg_host_pattern(const nbg_mesh_t *m, uint32_t *row_ptr, uint32_t *col_idx);
+
+/* Node -> (element, local node) incidence in ascending element order. */
+int nbg_host_incidence(const nbg_mesh_t *m, uint32_t *inc_ptr, uint32_t *inc_elem,
+                       uint8_t *inc_local);
+
+/* Device-resident FEM system of one mesh: pattern, K, F, u, strain. */
+typedef struct nbg_fem nbg_fem_t;
+
+int nbg_fem_create(nbg_fem_t **out, const nbg_mesh_t *m, void *stream);
+void nbg_fem_destroy(nbg_fem_t *f);
+uint32_t nbg_fem_n_dof(const nbg_fem_t *f);
+uint64_t nbg_fem_nnz(const nbg_fem_t *f);
+/* pipeline_assemble_system with one modulus per element (host arrays;
+ * enabled may be NULL).  Returns 0, NBG_DISTORTED, or an error. */
+int nbg_fem_assemble(nbg_fem_t *f, const double *E, double nu, double thickness,
+                     double density, int self_weight, const double gravity[2],
+                     const uint8_t *enabled);
+/* nb_fem_set_bconditions(mesh, K, F, bcond, factor) */
+int nbg_fem_apply_bcs(nbg_fem_t *f, const nbg_bcs_t *b, double factor);
+/* Jacobi-PCG on the assembled system, x0 = 0 (static_elasticity2D.c:83-97). */
+int nbg_fem_solve(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
+                  nbg_cg_result_t *res);
+/* The block layout of K (refilled from the current K values). */
+int nbg_fem_block_layout(nbg_fem_t *f, nbg_bsr_t *out);
+/* Fast FP64 CG and mixed-precision CG on the assembled system, x0 = 0. */
+int nbg_fem_solve_fast(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
+                       nbg_cg_result_t *res);
+int nbg_fem_solve_mixed(nbg_fem_t *f, uint32_t max_iter, double tol, double delta,
+                        unsigned flags, nbg_mixed_result_t *res);
+int nbg_fem_strain(nbg_fem_t *f);
+int nbg_fem_stress(nbg_fem_t *f);
+
+#define NBG_FEM_ROW_PTR 0   /* uint32[N+1] */
+#define NBG_FEM_COL_IDX 1   /* uint32[nnz] */
+#define NBG_FEM_K 2         /* double[nnz] */
+#define NBG_FEM_F 3         /* double[N] */
+#define NBG_FEM_U 4         /* double[N] */
+#define NBG_FEM_STRAIN 5    /* double[3 N_gp N_elem] */
+#define NBG_FEM_STRESS 6    /* double[3 N_gp N_elem] */
+#define NBG_FEM_E 7         /* double[N_elem] */
+/* Device pointer of one array, and a copy of it to host memory. */
+void *nbg_fem_device_ptr(nbg_fem_t *f, int what);
+size_t nbg_fem_bytes(const nbg_fem_t *f, int what);
+int nbg_fem_download(nbg_fem_t *f, int what, void *host);
+int nbg_fem_upload(nbg_fem_t *f, int what, const void *host);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

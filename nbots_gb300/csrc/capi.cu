@@ -1,0 +1,70 @@
+// Library-wide pieces of the C ABI: version, error text, device memory.
+#include <cstdio>
+#include <cstring>
+
+#include "common.cuh"
+
+namespace {
+thread_local char g_last_error[256] = "";
+}
+
+int nbg_cuda_error(cudaError_t e) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s: %s", cudaGetErrorName(e),
+                  cudaGetErrorString(e));
+    if (e == cudaErrorMemoryAllocation) return NBG_ERR_NOMEM;
+    return NBG_ERR_CUDA;
+}
+
+extern "C" const char* nbg_version(void) { return "nbots_gb300 0.1 (sm_103a)"; }
+
+extern "C" const char* nbg_last_error(void) { return g_last_error; }
+
+extern "C" int nbg_device_count(void) {
+    int n = 0;
+    if (cudaGetDeviceCount(&n) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return n;
+}
+
+extern "C" int nbg_dev_alloc(void** ptr, size_t bytes) {
+    if (!ptr) return NBG_ERR_ARG;
+    *ptr = nullptr;
+    NBG_CHECK(cudaMalloc(ptr, bytes ? bytes : 1));
+    return NBG_OK;
+}
+
+extern "C" int nbg_dev_free(void* ptr) {
+    if (ptr) NBG_CHECK(cudaFree(ptr));
+    return NBG_OK;
+}
+
+extern "C" int nbg_h2d(void* dst, const void* src, size_t bytes, void* stream) {
+    if (bytes == 0) return NBG_OK;
+    NBG_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyHostToDevice, (cudaStream_t)stream));
+    return NBG_OK;
+}
+
+extern "C" int nbg_d2h(void* dst, const void* src, size_t bytes, void* stream) {
+    if (bytes == 0) return NBG_OK;
+    NBG_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToHost, (cudaStream_t)stream));
+    return NBG_OK;
+}
+
+extern "C" int nbg_stream_sync(void* stream) {
+    NBG_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
+    return NBG_OK;
+}
+
+extern "C" int nbg_host_alloc(void** ptr, size_t bytes) {
+    if (!ptr) return NBG_ERR_ARG;
+    *ptr = nullptr;
+    NBG_CHECK(cudaMallocHost(ptr, bytes ? bytes : 1));
+    return NBG_OK;
+}
+
+extern "C" int nbg_host_free(void* ptr) {
+    if (ptr) NBG_CHECK(cudaFreeHost(ptr));
+    return NBG_OK;
+}

@@ -1,0 +1,300 @@
+// Persistent FP64 (Jacobi-preconditioned) CG: one cooperative launch runs
+// the whole solve with device-side convergence checks.
+//
+// Iteration (nbots' cg_precond_jacobi.c:45-76):
+//   L1: w = A p; dot_pw, dot_gg (old g), dot_gq
+//   L2: alpha = gq/pw; x += alpha p; g += alpha w; q = g / Aii; dot_gkqk
+//   L3: beta = gkqk/gq; p = -q + beta p
+// Here L3 is folded into the next L1: every block forms p_k = -q + beta
+// p_{k-1} for its own rows (written to the other half of a double buffer)
+// and recomputes the same expression, bit for bit, for the columns it
+// gathers.  That leaves two grid barriers per iteration.  Per-row work
+// repeats nbots' arithmetic (rounded products, left-to-right row sums,
+// division by the diagonal); the dot products are block-tree plus a fixed
+// block order, identical from run to run.
+#include <cstdint>
+
+#include "common.cuh"
+
+using namespace nbg;
+
+namespace {
+
+constexpr int kThreads = 256;
+
+struct CgDevResult {
+    uint32_t niter;
+    int status;
+    double dot_gg;
+    double bb;
+};
+
+struct CgArgs {
+    uint32_t N;
+    const uint32_t* rp;
+    const uint32_t* ci;
+    const double* val;
+    const double* b;
+    double* x;
+    double* g;
+    double* q;
+    double* P0;
+    double* P1;
+    double* w;
+    double* Aii;
+    double* partA;  // 3 per block
+    double* partB;  // 1 per block
+    double* partC;  // 2 per block
+    unsigned* bar;
+    int* status;
+    CgDevResult* res;
+    uint32_t max_iter;
+    double tol;
+    unsigned flags;
+};
+
+// Sum of NV partials per block over all blocks in block order; every block
+// gets the same bits.
+template <int NV>
+__device__ __forceinline__ void grid_reduce(const double* part, double* out, double* sh) {
+    const unsigned G = gridDim.x;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (unsigned b = lane; b < G; b += 32) s = add(s, part[b * NV + k]);
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s = add(s, __shfl_down_sync(0xffffffffu, s, o));
+            if (lane == 0) sh[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = sh[k];
+    __syncthreads();
+}
+
+template <bool JAC>
+__global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
+    __shared__ double red[3 * 32];
+    __shared__ double bc[4];
+    const unsigned G = gridDim.x;
+    const uint32_t per = (a.N + G - 1) / G;
+    const uint32_t r0 = min(blockIdx.x * per, a.N), r1 = min(r0 + per, a.N);
+    const uint32_t* __restrict__ rp = a.rp;
+    const uint32_t* __restrict__ ci = a.ci;
+    const double* __restrict__ val = a.val;
+
+    // init (cg_precond_jacobi.c:33-43)
+    {
+        double v[2] = {0.0, 0.0};
+        for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+            double sum = 0.0, d = 0.0;
+            for (uint32_t k = rp[r]; k < rp[r + 1]; k++) {
+                const uint32_t c = ci[k];
+                sum = add(sum, mul(val[k], a.x[c]));
+                if (c == r) d = val[k];
+            }
+            const double gi = sub(sum, a.b[r]);
+            const double qi = JAC ? dvd(gi, d) : gi;
+            a.g[r] = gi;
+            a.Aii[r] = d;
+            a.q[r] = qi;
+            a.P0[r] = -qi;
+            v[0] = add(v[0], mul(gi, gi));
+            v[1] = add(v[1], mul(a.b[r], a.b[r]));
+        }
+        block_sum<2>(v, red);
+        if (threadIdx.x == 0) {
+            a.partC[blockIdx.x * 2] = v[0];
+            a.partC[blockIdx.x * 2 + 1] = v[1];
+        }
+    }
+    uint32_t k = 0;
+    double dot_gg = 0.0, bb = 0.0;
+    if (grid_barrier(a.bar, G, a.status)) goto done;
+    {
+        double t[2];
+        grid_reduce<2>(a.partC, t, bc);
+        dot_gg = t[0];
+        bb = t[1];
+    }
+    {
+        const double tolb = (a.flags & NBG_CG_RELATIVE) ? a.tol * sqrt(bb) : a.tol;
+        const double tol2 = tolb * tolb;
+        double beta = 0.0;
+        while (dot_gg > tol2 && k < a.max_iter) {
+            double* __restrict__ pk = (k & 1) ? a.P1 : a.P0;
+            const double* __restrict__ pprev = (k & 1) ? a.P0 : a.P1;
+            const double* __restrict__ q = a.q;
+            // L1 with the p update of the previous L3 folded in
+            double v3[3] = {0.0, 0.0, 0.0};
+            for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+                double pr, s = 0.0;
+                if (k == 0) {
+                    pr = pk[r];
+                    for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++)
+                        s = add(s, mul(val[kk], pk[ci[kk]]));
+                } else {
+                    pr = add(-q[r], mul(beta, pprev[r]));
+                    pk[r] = pr;
+                    for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++) {
+                        const uint32_t c = ci[kk];
+                        s = add(s, mul(val[kk], add(-q[c], mul(beta, pprev[c]))));
+                    }
+                }
+                a.w[r] = s;
+                const double gi = a.g[r], qi = q[r];
+                v3[0] = add(v3[0], mul(pr, s));
+                v3[1] = add(v3[1], mul(gi, gi));
+                v3[2] = add(v3[2], mul(gi, qi));
+            }
+            block_sum<3>(v3, red);
+            if (threadIdx.x == 0) {
+                a.partA[blockIdx.x * 3] = v3[0];
+                a.partA[blockIdx.x * 3 + 1] = v3[1];
+                a.partA[blockIdx.x * 3 + 2] = v3[2];
+            }
+            if (grid_barrier(a.bar, G, a.status)) goto done;
+            double t3[3];
+            grid_reduce<3>(a.partA, t3, bc);
+            const double dot_pw = t3[0], dot_gq = t3[2];
+            dot_gg = t3[1];
+            const double alpha = dvd(dot_gq, dot_pw);
+            // L2
+            double v1[1] = {0.0};
+            for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+                a.x[r] = add(a.x[r], mul(alpha, pk[r]));
+                const double gi = add(a.g[r], mul(alpha, a.w[r]));
+                a.g[r] = gi;
+                const double qi = JAC ? dvd(gi, a.Aii[r]) : gi;
+                a.q[r] = qi;
+                v1[0] = add(v1[0], mul(gi, qi));
+            }
+            block_sum<1>(v1, red);
+            if (threadIdx.x == 0) a.partB[blockIdx.x] = v1[0];
+            if (grid_barrier(a.bar, G, a.status)) goto done;
+            double t1[1];
+            grid_reduce<1>(a.partB, t1, bc);
+            beta = dvd(t1[0], dot_gq);
+            k++;
+        }
+    }
+done:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        const double tolb = (a.flags & NBG_CG_RELATIVE) ? a.tol * sqrt(bb) : a.tol;
+        a.res->niter = k;
+        a.res->dot_gg = dot_gg;
+        a.res->bb = bb;
+        int st = ld_volatile(a.status);
+        a.res->status = st != 0 ? st : (dot_gg > tolb * tolb ? NBG_NOT_CONVERGED : NBG_OK);
+    }
+}
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+constexpr unsigned kMaxBlocks = 4096;
+
+struct Layout {
+    size_t g, q, P0, P1, w, Aii, partA, partB, partC, bar, status, res, total;
+};
+
+Layout layout(uint32_t N) {
+    Layout L;
+    size_t o = 0;
+    const size_t v = align256((size_t)N * 8);
+    L.g = o; o += v;
+    L.q = o; o += v;
+    L.P0 = o; o += v;
+    L.P1 = o; o += v;
+    L.w = o; o += v;
+    L.Aii = o; o += v;
+    L.partA = o; o += align256(kMaxBlocks * 3 * 8);
+    L.partB = o; o += align256(kMaxBlocks * 8);
+    L.partC = o; o += align256(kMaxBlocks * 2 * 8);
+    L.bar = o; o += 256;
+    L.status = o; o += 256;
+    L.res = o; o += 256;
+    L.total = o;
+    return L;
+}
+
+}  // namespace
+
+extern "C" size_t nbg_cg_workspace_bytes(uint32_t N) { return layout(N).total; }
+
+extern "C" int nbg_cg_f64(uint32_t N, const uint32_t* row_ptr, const uint32_t* col_idx,
+                          const double* val, const double* b, double* x, uint32_t max_iter,
+                          double tol, unsigned flags, nbg_cg_result_t* result, void* ws,
+                          size_t ws_bytes, void* stream) {
+    if (!result) return NBG_ERR_ARG;
+    result->niter = 0;
+    result->status = NBG_OK;
+    result->tol_reached = 0.0;
+    result->bnorm = 0.0;
+    if (N == 0) return NBG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    const Layout L = layout(N);
+    void* own = nullptr;
+    if (ws == nullptr) {
+        NBG_CHECK(cudaMalloc(&own, L.total));
+        ws = own;
+    } else if (ws_bytes < L.total) {
+        return NBG_ERR_ARG;
+    }
+    char* base = (char*)ws;
+    CgArgs a;
+    a.N = N;
+    a.rp = row_ptr;
+    a.ci = col_idx;
+    a.val = val;
+    a.b = b;
+    a.x = x;
+    a.g = (double*)(base + L.g);
+    a.q = (double*)(base + L.q);
+    a.P0 = (double*)(base + L.P0);
+    a.P1 = (double*)(base + L.P1);
+    a.w = (double*)(base + L.w);
+    a.Aii = (double*)(base + L.Aii);
+    a.partA = (double*)(base + L.partA);
+    a.partB = (double*)(base + L.partB);
+    a.partC = (double*)(base + L.partC);
+    a.bar = (unsigned*)(base + L.bar);
+    a.status = (int*)(base + L.status);
+    a.res = (CgDevResult*)(base + L.res);
+    a.max_iter = max_iter;
+    a.tol = tol;
+    a.flags = flags;
+
+    int rc = NBG_OK;
+    cudaError_t e = cudaMemsetAsync(base + L.bar, 0, 3 * 256, s);
+    int dev = 0, nsm = 0, occ = 0;
+    const void* fn = (flags & NBG_CG_JACOBI) ? (const void*)k_cg_f64<true> : (const void*)k_cg_f64<false>;
+    if (e == cudaSuccess) e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreads, 0);
+    CgDevResult hr{};
+    if (e == cudaSuccess) {
+        unsigned G = (unsigned)(nsm * (occ < 2 ? occ : 2));
+        const unsigned want = (N + kThreads * 4 - 1) / (kThreads * 4);
+        if (want < G) G = want;
+        if (G < 1) G = 1;
+        if (G > kMaxBlocks) G = kMaxBlocks;
+        void* args[] = {&a};
+        e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kThreads), args, 0, s);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(&hr, a.res, sizeof(hr), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) {
+        rc = nbg_cuda_error(e);
+    } else {
+        result->niter = hr.niter;
+        result->status = hr.status;
+        result->tol_reached = sqrt(hr.dot_gg);
+        result->bnorm = sqrt(hr.bb);
+        rc = hr.status;
+    }
+    if (own) cudaFree(own);
+    return rc;
+}

@@ -1,0 +1,208 @@
+// Fast persistent FP64 Jacobi-PCG on the 2x2-block SELL layout (bsr.cu):
+// one cooperative launch per solve, one thread per node row, convergence
+// decided on the device, every spin bounded.
+//
+// GB300 issues FP64 at a small fraction of its FP32 rate, so this kernel
+// keeps the FP64 instruction count at one FMA per stored value plus seven
+// per dof (q = g / Aii becomes a multiply by the stored reciprocal, and
+// dot_gq of the next L1 reuses dot_gkqk of L2) and uses three barriers per
+// iteration, one after each of L1 | L2 | L3 of cg_precond_jacobi.c:50-74.
+// The stop test uses the current gradient norm, not nbots' lagged one.
+#include <cstdint>
+
+#include "persist.cuh"
+
+using namespace nbg;
+
+namespace {
+
+struct CgBsrArgs {
+    nbg_bsr_t A;
+    const double* b;
+    double* x;
+    double *g, *q, *p, *w;
+    double* part;  // 6 * kMaxBlocks doubles: L1 [0,K), L2 [K,3K), init [3K,6K)
+    unsigned* bar;
+    int* status;
+    double* res;  // niter, status, gg, bb
+    uint32_t max_iter;
+    double tol;
+    unsigned flags;
+};
+
+__global__ void __launch_bounds__(kPersistThreads) k_cg_bsr_f64(CgBsrArgs a) {
+    __shared__ double red[3 * 32];
+    __shared__ double bc[3];
+    const unsigned G = gridDim.x;
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nw = kPersistThreads / 32;
+    uint32_t s0, s1;
+    slice_range(a.A.n_slices, s0, s1);
+    const uint32_t Nn = a.A.Nn;
+    double2* __restrict__ x = reinterpret_cast<double2*>(a.x);
+    double2* __restrict__ g = reinterpret_cast<double2*>(a.g);
+    double2* __restrict__ q = reinterpret_cast<double2*>(a.q);
+    double2* __restrict__ p = reinterpret_cast<double2*>(a.p);
+    double2* __restrict__ w = reinterpret_cast<double2*>(a.w);
+    const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
+    const double2* __restrict__ dinv = reinterpret_cast<const double2*>(a.A.dinv64);
+
+    {   // init: g = A x - b, q = g / Aii, p = -q
+        double v[3] = {0.0, 0.0, 0.0};  // gq, gg, bb
+        for (uint32_t s = s0 + warp; s < s1; s += nw) {
+            const uint32_t i = s * 32 + lane;
+            if (i >= Nn) continue;
+            const double2 ax = spmv_row_f64(a.A, s, lane, x);
+            const double2 bi = b[i], di = dinv[i];
+            const double2 gi = make_double2(ax.x - bi.x, ax.y - bi.y);
+            const double2 qi = make_double2(gi.x * di.x, gi.y * di.y);
+            g[i] = gi;
+            q[i] = qi;
+            p[i] = make_double2(-qi.x, -qi.y);
+            v[0] = fma(gi.x, qi.x, fma(gi.y, qi.y, v[0]));
+            v[1] = fma(gi.x, gi.x, fma(gi.y, gi.y, v[1]));
+            v[2] = fma(bi.x, bi.x, fma(bi.y, bi.y, v[2]));
+        }
+        publish<3>(v, red, a.part + 3 * kMaxBlocks);  // own slot: L1 may overwrite [0, G) early
+    }
+    uint32_t k = 0;
+    double gq = 0.0, gg = 0.0, bb = 0.0, target2 = 0.0;
+    if (grid_barrier(a.bar, G, a.status)) goto done;
+    {
+        double t[3];
+        grid_reduce<3>(a.part + 3 * kMaxBlocks, t, bc);
+        gq = t[0];
+        gg = t[1];
+        bb = t[2];
+    }
+    target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * bb : a.tol * a.tol;
+    while (gg > target2 && k < a.max_iter) {
+        {   // L1: w = A p, p.w
+            double v[1] = {0.0};
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane;
+                if (i >= Nn) continue;
+                const double2 wi = spmv_row_f64(a.A, s, lane, p);
+                w[i] = wi;
+                const double2 pi = p[i];
+                v[0] = fma(pi.x, wi.x, fma(pi.y, wi.y, v[0]));
+            }
+            publish<1>(v, red, a.part);
+        }
+        if (grid_barrier(a.bar, G, a.status)) goto done;
+        double pw;
+        grid_reduce<1>(a.part, &pw, bc);
+        const double alpha = gq / pw;
+        {   // L2: x += alpha p, g += alpha w, q = g / Aii
+            double v[2] = {0.0, 0.0};
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane;
+                if (i >= Nn) continue;
+                const double2 pi = p[i], wi = w[i], di = dinv[i];
+                double2 xi = x[i], gi = g[i];
+                xi.x = fma(alpha, pi.x, xi.x);
+                xi.y = fma(alpha, pi.y, xi.y);
+                gi.x = fma(alpha, wi.x, gi.x);
+                gi.y = fma(alpha, wi.y, gi.y);
+                const double2 qi = make_double2(gi.x * di.x, gi.y * di.y);
+                x[i] = xi;
+                g[i] = gi;
+                q[i] = qi;
+                v[0] = fma(gi.x, qi.x, fma(gi.y, qi.y, v[0]));
+                v[1] = fma(gi.x, gi.x, fma(gi.y, gi.y, v[1]));
+            }
+            publish<2>(v, red, a.part + kMaxBlocks);
+        }
+        if (grid_barrier(a.bar, G, a.status)) goto done;
+        double t2[2];
+        grid_reduce<2>(a.part + kMaxBlocks, t2, bc);
+        const double beta = t2[0] / gq;
+        gq = t2[0];
+        gg = t2[1];
+        k++;
+        if (!(gg > target2) || k >= a.max_iter) break;
+        // L3: p = -q + beta p
+        for (uint32_t s = s0 + warp; s < s1; s += nw) {
+            const uint32_t i = s * 32 + lane;
+            if (i >= Nn) continue;
+            const double2 qi = q[i], pi = p[i];
+            p[i] = make_double2(fma(beta, pi.x, -qi.x), fma(beta, pi.y, -qi.y));
+        }
+        if (grid_barrier(a.bar, G, a.status)) goto done;
+    }
+done:
+    if (blockIdx.x == 0 && threadIdx.x == 0) {
+        a.res[0] = (double)k;
+        int st = ld_volatile(a.status);
+        a.res[1] = st != 0 ? (double)st : (gg > target2 ? 1.0 : 0.0);
+        a.res[2] = gg;
+        a.res[3] = bb;
+    }
+}
+
+size_t cg_bsr_bytes(uint32_t N) {
+    return 4 * align256((size_t)N * 8) + align256(kMaxBlocks * 3 * 8) * 2 + 3 * 256;
+}
+
+}  // namespace
+
+extern "C" size_t nbg_cg_bsr_workspace_bytes(uint32_t N) { return cg_bsr_bytes(N); }
+
+extern "C" int nbg_cg_bsr_f64(const nbg_bsr_t* A, const double* b, double* x, uint32_t max_iter,
+                              double tol, unsigned flags, nbg_cg_result_t* result, void* ws,
+                              size_t ws_bytes, void* stream) {
+    if (!result || !A) return NBG_ERR_ARG;
+    *result = nbg_cg_result_t{0, 0, 0.0, 0.0};
+    if (A->Nn == 0) return NBG_OK;
+    if (!A->b64 || !A->dinv64) return NBG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const size_t need = cg_bsr_bytes(A->N);
+    void* own = nullptr;
+    if (!ws) {
+        NBG_CHECK(cudaMalloc(&own, need));
+        ws = own;
+    } else if (ws_bytes < need) {
+        return NBG_ERR_ARG;
+    }
+    char* base = (char*)ws;
+    const size_t v = align256((size_t)A->N * 8);
+    CgBsrArgs a;
+    a.A = *A;
+    a.b = b;
+    a.x = x;
+    a.g = (double*)(base);
+    a.q = (double*)(base + v);
+    a.p = (double*)(base + 2 * v);
+    a.w = (double*)(base + 3 * v);
+    a.part = (double*)(base + 4 * v);
+    char* tail = base + 4 * v + 2 * align256(kMaxBlocks * 3 * 8);
+    a.bar = (unsigned*)tail;
+    a.status = (int*)(tail + 256);
+    a.res = (double*)(tail + 512);
+    a.max_iter = max_iter;
+    a.tol = tol;
+    a.flags = flags;
+    int rc = NBG_OK;
+    unsigned G = 1;
+    double hr[4] = {0, 0, 0, 0};
+    cudaError_t e = cudaMemsetAsync(tail, 0, 3 * 256, s);
+    if (e == cudaSuccess) rc = coop_grid((const void*)k_cg_bsr_f64, A->n_slices, &G);
+    if (e == cudaSuccess && rc == NBG_OK) {
+        void* args[] = {&a};
+        e = cudaLaunchCooperativeKernel((const void*)k_cg_bsr_f64, dim3(G), dim3(kPersistThreads),
+                                        args, 0, s);
+    }
+    if (e == cudaSuccess && rc == NBG_OK)
+        e = cudaMemcpyAsync(hr, a.res, sizeof(hr), cudaMemcpyDeviceToHost, s);
+    if (e == cudaSuccess && rc == NBG_OK) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = nbg_cuda_error(e);
+    if (rc == NBG_OK) {
+        result->niter = (uint32_t)hr[0];
+        result->status = (int)hr[1];
+        result->tol_reached = sqrt(hr[2]);
+        result->bnorm = sqrt(hr[3]);
+        rc = result->status;
+    }
+    if (own) cudaFree(own);
+    return rc;
+}

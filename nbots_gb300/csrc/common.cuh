@@ -1,0 +1,187 @@
+// Shared device helpers for the nbots GB300 kernels.
+//
+//  * exact FP64 helpers: nbots is built with -std=c99, i.e. GCC's
+//    -ffp-contract=off (CMakeLists.txt:33), so every product is rounded
+//    before it is added.  The parity kernels spell each operation with the
+//    _rn intrinsics, which nvcc never contracts into an FMA.
+//  * a bounded grid barrier for cooperative (co-resident) launches: every
+//    spin has a time limit; on expiry the kernel records NBG_ERR_TIMEOUT in
+//    a device status word and all blocks leave their loops.
+//  * fixed-order block reductions, so every run produces the same bits.
+#pragma once
+
+#include <cstdint>
+#include <cuda_runtime.h>
+#include <cuda_bf16.h>
+
+#include "nbots_gb300.h"
+
+#define NBG_CHECK(call)                                            \
+    do {                                                           \
+        cudaError_t e_ = (call);                                   \
+        if (e_ != cudaSuccess) return nbg_cuda_error(e_);          \
+    } while (0)
+
+int nbg_cuda_error(cudaError_t e);
+
+namespace nbg {
+
+__device__ __forceinline__ double mul(double a, double b) { return __dmul_rn(a, b); }
+__device__ __forceinline__ double add(double a, double b) { return __dadd_rn(a, b); }
+__device__ __forceinline__ double sub(double a, double b) { return __dsub_rn(a, b); }
+__device__ __forceinline__ double dvd(double a, double b) { return __ddiv_rn(a, b); }
+
+__device__ __forceinline__ uint64_t globaltimer() {
+    uint64_t t;
+    asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+    return t;
+}
+
+__device__ __forceinline__ unsigned ld_acquire(const unsigned* p) {
+    unsigned v;
+    asm volatile("ld.acquire.gpu.global.u32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+    return v;
+}
+
+__device__ __forceinline__ void st_release(unsigned* p, unsigned v) {
+    asm volatile("st.release.gpu.global.u32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+__device__ __forceinline__ int ld_volatile(const int* p) { return *(const volatile int*)p; }
+
+// Spin limit of every device-side wait (nanoseconds of %globaltimer).
+constexpr uint64_t kSpinLimitNs = 2000000000ull;
+
+// Grid-wide barrier: bar[0] arrival count, bar[1] generation.  Requires all
+// blocks to be co-resident (cooperative launch).  Returns nonzero when the
+// caller must stop (timeout here or an error recorded by another block).
+__device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
+    __shared__ int s_stop;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+        int stop = 0;
+        unsigned gen = ld_acquire(&bar[1]);
+        __threadfence();
+        unsigned prev = atomicAdd(&bar[0], 1u);
+        if (prev == nblocks - 1) {
+            atomicExch(&bar[0], 0u);
+            __threadfence();
+            st_release(&bar[1], gen + 1);
+        } else {
+            uint64_t t0 = globaltimer();
+            while (ld_acquire(&bar[1]) == gen) {
+                if (globaltimer() - t0 > kSpinLimitNs) {
+                    atomicCAS(status, 0, NBG_ERR_TIMEOUT);
+                    stop = 1;
+                    break;
+                }
+                __nanosleep(32);
+            }
+        }
+        if (!stop && ld_volatile(status) != 0) stop = 1;
+        s_stop = stop;
+    }
+    __syncthreads();
+    return s_stop;
+}
+
+// Block-wide sum of NV values per thread, fixed tree order.  Result valid in
+// thread 0.  `scratch` holds NV * 32 doubles.
+template <int NV>
+__device__ __forceinline__ void block_sum(double (&v)[NV], double* scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++) {
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] = add(v[k], __shfl_down_sync(0xffffffffu, v[k], o));
+    }
+    __syncthreads();
+    if (lane == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) scratch[k * 32 + warp] = v[k];
+    }
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = lane < nwarps ? scratch[k * 32 + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s = add(s, __shfl_down_sync(0xffffffffu, s, o));
+            v[k] = s;
+        }
+    }
+}
+
+// Float flavour with Kahan-compensated accumulation carried as (sum, comp).
+struct Kahan {
+    float s, c;
+    __device__ __forceinline__ void add(float x) {
+        float y = __fsub_rn(x, c);
+        float t = __fadd_rn(s, y);
+        c = __fsub_rn(__fsub_rn(t, s), y);
+        s = t;
+    }
+    __device__ __forceinline__ double value() const { return (double)s - (double)c; }
+};
+
+// Float-float (unevaluated sum hi + lo of two FP32 numbers) built from the
+// classic error-free transformations: Knuth's TwoSum, Dekker's FastTwoSum
+// and the FMA form of TwoProduct.  Every step is spelled with _rn
+// intrinsics so no contraction or reassociation can break them.
+struct FF {
+    float hi, lo;
+};
+
+__device__ __forceinline__ FF two_sum(float a, float b) {
+    const float s = __fadd_rn(a, b);
+    const float bb = __fsub_rn(s, a);
+    const float e = __fadd_rn(__fsub_rn(a, __fsub_rn(s, bb)), __fsub_rn(b, bb));
+    return {s, e};
+}
+
+__device__ __forceinline__ FF fast_two_sum(float a, float b) {  // |a| >= |b|
+    const float s = __fadd_rn(a, b);
+    return {s, __fsub_rn(b, __fsub_rn(s, a))};
+}
+
+__device__ __forceinline__ FF two_prod(float a, float b) {
+    const float p = __fmul_rn(a, b);
+    return {p, __fmaf_rn(a, b, -p)};
+}
+
+// Accumulator for sum_k (a_hi + a_lo)(x_hi + x_lo): the a_lo x_lo term is
+// below the working precision and dropped.
+struct FFAcc {
+    float s, c;
+    __device__ __forceinline__ void fma2(float ahi, float alo, float xhi, float xlo) {
+        FF p = two_prod(ahi, xhi);
+        float e = __fmaf_rn(ahi, xlo, p.lo);
+        e = __fmaf_rn(alo, xhi, e);
+        FF t = two_sum(s, p.hi);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, e));
+    }
+    __device__ __forceinline__ FF result() const { return fast_two_sum(s, c); }
+};
+
+__device__ __forceinline__ FF ff_from_double(double d) {
+    const float h = (float)d;
+    return {h, (float)(d - (double)h)};
+}
+
+// a + b for float-float operands
+__device__ __forceinline__ FF ff_add(FF a, FF b) {
+    FF s = two_sum(a.hi, b.hi);
+    return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
+}
+
+// a * b, both float-float
+__device__ __forceinline__ FF ff_mul(FF a, FF b) {
+    FF p = two_prod(a.hi, b.hi);
+    float e = __fmaf_rn(a.hi, b.lo, p.lo);
+    e = __fmaf_rn(a.lo, b.hi, e);
+    return fast_two_sum(p.hi, e);
+}
+
+}  // namespace nbg

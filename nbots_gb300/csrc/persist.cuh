@@ -1,0 +1,113 @@
+// Helpers shared by the persistent (one cooperative launch per solve)
+// solvers on the 2x2-block SELL layout: block-to-slice partition,
+// fixed-order block and grid reductions, FP64 block-row SpMV, launch sizing.
+#pragma once
+
+#include <cstdint>
+
+#include "common.cuh"
+
+namespace nbg {
+
+constexpr int kPersistThreads = 256;
+constexpr unsigned kMaxBlocks = 4096;
+
+inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
+
+// Contiguous, balanced slice range [s0, s1) of this block.
+__device__ __forceinline__ void slice_range(uint32_t S, uint32_t& s0, uint32_t& s1) {
+    s0 = (uint32_t)(((uint64_t)S * blockIdx.x) / gridDim.x);
+    s1 = (uint32_t)(((uint64_t)S * (blockIdx.x + 1)) / gridDim.x);
+}
+
+// Sum over blocks of NV partials per block, in block order; every block
+// computes the same bits.
+template <int NV>
+__device__ __forceinline__ void grid_reduce(const double* part, double* out, double* sh) {
+    const unsigned G = gridDim.x;
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (unsigned b = lane; b < G; b += 32) s += part[b * NV + k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0) sh[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = sh[k];
+    __syncthreads();
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sum_plain(double (&v)[NV], double* scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) v[k] += __shfl_down_sync(0xffffffffu, v[k], o);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) scratch[k * 32 + warp] = v[k];
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = lane < nwarps ? scratch[k * 32 + lane] : 0.0;
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            v[k] = s;
+        }
+    }
+}
+
+// Block sum, then thread 0 stores the NV results in this block's slot.
+template <int NV>
+__device__ __forceinline__ void publish(double (&v)[NV], double* red, double* part) {
+    block_sum_plain<NV>(v, red);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[blockIdx.x * NV + k] = v[k];
+}
+
+// (A x) for node row (s, lane) with FP64 values and FMAs.
+__device__ __forceinline__ double2 spmv_row_f64(const nbg_bsr_t& A, uint32_t s, uint32_t lane,
+                                                const double2* __restrict__ xv) {
+    const double2* __restrict__ bv = reinterpret_cast<const double2*>(A.b64);
+    double y0 = 0.0, y1 = 0.0;
+    const uint32_t k0 = A.slice_off[s], k1 = A.slice_off[s + 1];
+#pragma unroll 3
+    for (uint32_t k = k0; k < k1; k++) {
+        const size_t e = (size_t)k * 32 + lane;
+        const double2 xc = xv[A.bcol[e]];
+        const double2 top = bv[2 * e], bot = bv[2 * e + 1];
+        y0 = fma(top.x, xc.x, y0);
+        y0 = fma(top.y, xc.y, y0);
+        y1 = fma(bot.x, xc.x, y1);
+        y1 = fma(bot.y, xc.y, y1);
+    }
+    return make_double2(y0, y1);
+}
+
+// Grid size of a cooperative launch: every co-resident block, but not more
+// blocks than warps of slices.
+inline int coop_grid(const void* fn, uint32_t n_slices, unsigned* G) {
+    int dev = 0, nsm = 0, occ = 0;
+    NBG_CHECK(cudaGetDevice(&dev));
+    NBG_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, 0));
+    unsigned g = (unsigned)nsm * (unsigned)(occ > 0 ? occ : 1);
+    const unsigned want = (n_slices + kPersistThreads / 32 - 1) / (kPersistThreads / 32);
+    if (want < g) g = want;
+    if (g < 1) g = 1;
+    if (g > kMaxBlocks) g = kMaxBlocks;
+    *G = g;
+    return NBG_OK;
+}
+
+}  // namespace nbg
