@@ -1,0 +1,177 @@
+/*
+ * Drop-in replacements for nbots' FEM hot path (vecn/nbots), implemented in
+ * libnbots_gpu.so on the sm_103a kernels of include/nbots_gb300.h.
+ *
+ * Link libnbots_gpu.so ahead of libnbots.so (or LD_PRELOAD it): the symbols
+ * below then resolve to the GPU versions for every caller, including calls
+ * from inside libnbots, while the rest of nbots keeps working.  The
+ * signatures, argument meanings and return codes are nbots' own; each
+ * declaration cites the reference it replaces (paths relative to the nbots
+ * tree).  Differences are listed where they exist.
+ *
+ * The FEM entry reads meshes, boundary conditions, materials and element
+ * types only through nbots' public accessors (declared at the end).  Those
+ * come from libnbots.so in a real deployment; libnbots_host.so provides a
+ * standalone implementation of the same accessors (plus array constructors,
+ * nbh_*) for programs and tests without nbots.
+ */
+#ifndef NBOTS_DROPIN_H
+#define NBOTS_DROPIN_H
+
+#include <stdbool.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ----------------------------------------------------------- nbots types */
+/* headers/nb/graph_bot/graph.h:25-31 (public struct) */
+typedef struct {
+	uint32_t N;
+	uint32_t *N_adj;
+	uint32_t **adj;
+	double *wi;
+	double **wij;
+} nb_graph_t;
+
+/* sources/nb/solver_bot/sparse/sparse_struct.h:6-11; the drop-in keeps this
+ * layout (rows of pointers) so code that walks rows directly still works.
+ * nb_sparse_create backs all rows with two contiguous slabs, which the GPU
+ * path uploads without copying row by row. */
+typedef struct nb_sparse_s {
+	double **rows_values;
+	uint32_t **rows_index;
+	uint32_t *rows_size;
+	uint32_t N;
+} nb_sparse_t;
+
+/* opaque nbots objects (headers/nb/geometric_bot/mesh/mesh2D.h:14,
+ * headers/nb/pde_bot/boundary_conditions/bcond.h:17,
+ * headers/nb/pde_bot/material.h, headers/nb/pde_bot/finite_element/element.h:6) */
+typedef struct nb_mesh2D_s nb_mesh2D_t;
+typedef struct nb_bcond_s nb_bcond_t;
+typedef struct nb_bcond_iter_s nb_bcond_iter_t;
+typedef struct nb_material_s nb_material_t;
+typedef struct nb_fem_elem_s nb_fem_elem_t;
+
+typedef enum { NB_DIRICHLET, NB_NEUMANN } nb_bcond_id;           /* bcond.h:7-10 */
+typedef enum { NB_BC_ON_POINT, NB_BC_ON_SEGMENT } nb_bcond_where; /* bcond.h:12-15 */
+typedef enum { NB_TRG_LINEAR, NB_QUAD_LINEAR } nb_elem_id;        /* element.h:8-11 */
+typedef enum {                                                    /* analysis2D.h:4-8 */
+	NB_PLANE_STRESS,
+	NB_PLANE_STRAIN,
+	NB_SOLID_OF_REVOLUTION
+} nb_analysis2D_t;
+typedef struct {                                                  /* analysis2D.h:10-14 */
+	double thickness;
+	double revolution_axe;
+	char revolution_coordinate;
+} nb_analysis2D_params;
+
+/* ------------------------------------------------------- replaced: sparse */
+/* sparse.h:28-30, sparse.c:20-60 */
+nb_sparse_t *nb_sparse_create(const nb_graph_t *graph, const uint32_t *perm,
+			      uint32_t vars_per_node);
+/* sparse.h:32, sparse.c:78-95 */
+nb_sparse_t *nb_sparse_clone(nb_sparse_t *A);
+/* sparse.h:34, sparse.c:114-125: also frees rows other code allocated */
+void nb_sparse_destroy(nb_sparse_t *A);
+void nb_sparse_reset(nb_sparse_t *A);                                    /* sparse.c:127-132 */
+/* sparse.c:134-171, 186-219: per-row binary search (sparse_struct.c:7-20).
+ * nbots exits on a missing entry; the drop-in prints the same message,
+ * records the error (nbg_dropin_error) and leaves the matrix unchanged. */
+void nb_sparse_set(nb_sparse_t *A, uint32_t i, uint32_t j, double value);
+double nb_sparse_get(const nb_sparse_t *A, uint32_t i, uint32_t j);
+double nb_sparse_get_and_set(nb_sparse_t *A, uint32_t i, uint32_t j, double value);
+bool nb_sparse_is_non_zero(const nb_sparse_t *A, uint32_t i, uint32_t j);
+void nb_sparse_add(nb_sparse_t *A, uint32_t i, uint32_t j, double value);
+uint32_t nb_sparse_get_size(const nb_sparse_t *A);                      /* sparse.c:342-345 */
+uint32_t nb_sparse_get_nnz(const nb_sparse_t *A);                       /* sparse.c:348-354 */
+/* sparse.h:54-55, sparse.c:405-414: y = A x on the GPU in nbots' per-row
+ * order without FMA, so the result is bit-identical.  omp_parallel_threads
+ * is accepted and ignored. */
+void nb_sparse_multiply_vector(const nb_sparse_t *A, const double *in, double *out,
+			       uint32_t omp_parallel_threads);
+/* sparse.h:58-59, sparse.c:416-430 (host side, same order) */
+void nb_sparse_set_Dirichlet_condition(nb_sparse_t *A, double *RHS, uint32_t idx,
+				       double value);
+
+/* ------------------------------------------------------- replaced: solvers */
+/* headers/nb/solver_bot/sparse/solvers/cg_precond_jacobi.h:8-15,
+ * cg_precond_jacobi.c:13-90: nbots' iteration (g = Ax - b, absolute tolerance,
+ * lagged stop test) in one persistent GPU kernel.  Returns 0 or 1 (tolerance
+ * not reached) like nbots, or a negative nbg status on a GPU error. */
+int nb_sparse_solve_CG_precond_Jacobi(const nb_sparse_t *A, const double *b, double *x,
+				      uint32_t max_iter, double tolerance,
+				      uint32_t *niter_performed, double *tolerance_reached,
+				      uint32_t omp_parallel_threads);
+/* solvers/conjugate_gradient.h, conjugate_gradient.c:13-77 */
+int nb_sparse_solve_conjugate_gradient(const nb_sparse_t *A, const double *b, double *x,
+				       uint32_t max_iter, double tolerance,
+				       uint32_t *niter_performed, double *tolerance_reached,
+				       uint32_t omp_parallel_threads);
+
+/* ---------------------------------------------------------- replaced: FEM */
+/* headers/nb/pde_bot/finite_element/solid_mechanics/static_elasticity2D.h:13-24,
+ * static_elasticity2D.c:31-97: pattern, assembly, boundary conditions,
+ * Jacobi-PCG (x0 = 0, max_iter = N, tol 1e-8) and strain, all on the GPU.
+ * Returns 0, 1 (distorted element) like nbots, or a negative nbg status.
+ * Like nbots, every analysis type is computed as plane stress (the switch in
+ * formulas.c:32-46 falls through). */
+int nb_fem_compute_2D_Solid_Mechanics(const nb_mesh2D_t *part, const nb_fem_elem_t *elemtype,
+				      const nb_material_t *material, const nb_bcond_t *bcond,
+				      bool enable_self_weight, double gravity[2],
+				      nb_analysis2D_t analysis2D, nb_analysis2D_params *params2D,
+				      const bool *elements_enabled, double *displacement,
+				      double *strain);
+/* static_elasticity2D.h:26-32, static_elasticity2D.c:99-127 */
+void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t *elemtype,
+				       const nb_material_t *material, nb_analysis2D_t analysis2D,
+				       double *strain, const bool *elements_enabled,
+				       double *stress);
+
+/* Last error of a drop-in call that nbots would have ended with exit(1)
+ * (0 if none); cleared by reading. */
+int nbg_dropin_error(void);
+
+/* ---------------------------------------- consumed: nbots public accessors */
+uint32_t nb_mesh2D_get_N_nodes(const nb_mesh2D_t *mesh);
+uint32_t nb_mesh2D_get_N_edges(const nb_mesh2D_t *mesh);
+uint32_t nb_mesh2D_get_N_elems(const nb_mesh2D_t *mesh);
+uint32_t nb_mesh2D_get_N_invtx(const nb_mesh2D_t *mesh);
+uint32_t nb_mesh2D_get_N_insgm(const nb_mesh2D_t *mesh);
+double nb_mesh2D_node_get_x(const nb_mesh2D_t *mesh, uint32_t id);
+double nb_mesh2D_node_get_y(const nb_mesh2D_t *mesh, uint32_t id);
+uint32_t nb_mesh2D_edge_get_1n(const nb_mesh2D_t *mesh, uint32_t id);
+uint32_t nb_mesh2D_edge_get_2n(const nb_mesh2D_t *mesh, uint32_t id);
+uint32_t nb_mesh2D_elem_get_adj(const nb_mesh2D_t *mesh, uint32_t elem_id, uint8_t adj_id);
+uint32_t nb_mesh2D_get_invtx(const nb_mesh2D_t *mesh, uint32_t id);
+uint32_t nb_mesh2D_insgm_get_N_nodes(const nb_mesh2D_t *mesh, uint32_t id);
+uint32_t nb_mesh2D_insgm_get_node(const nb_mesh2D_t *mesh, uint32_t sgm_id, uint32_t node_id);
+
+uint16_t nb_bcond_iter_get_memsize(void);
+void nb_bcond_iter_init(void *iter_ptr);
+void nb_bcond_iter_finish(void *iter_ptr);
+void nb_bcond_iter_set_conditions(nb_bcond_iter_t *iter, const nb_bcond_t *bcond,
+				  nb_bcond_id type_id, nb_bcond_where type_elem);
+bool nb_bcond_iter_has_more(const nb_bcond_iter_t *iter);
+void nb_bcond_iter_go_next(nb_bcond_iter_t *iter);
+uint32_t nb_bcond_iter_get_id(const nb_bcond_iter_t *iter);
+bool nb_bcond_iter_get_mask(const nb_bcond_iter_t *iter, uint8_t dof_id);
+bool nb_bcond_iter_val_is_function(const nb_bcond_iter_t *iter);
+void nb_bcond_iter_get_val(const nb_bcond_iter_t *iter, uint8_t N_dof, double *x, double t,
+			   double val[]);
+uint8_t nb_bcond_get_N_dof(const nb_bcond_t *bcond);
+
+double nb_material_get_elasticity_module(const nb_material_t *mat);
+double nb_material_get_poisson_module(const nb_material_t *mat);
+double nb_material_get_density(const nb_material_t *mat);
+
+uint8_t nb_fem_elem_get_N_nodes(const nb_fem_elem_t *elemtype);
+uint8_t nb_fem_elem_get_N_gpoints(const nb_fem_elem_t *elemtype);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

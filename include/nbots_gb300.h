@@ -46,6 +46,10 @@ int nbg_dev_free(void *ptr);
 int nbg_h2d(void *dst, const void *src, size_t bytes, void *stream);
 int nbg_d2h(void *dst, const void *src, size_t bytes, void *stream);
 int nbg_stream_sync(void *stream);
+/* Device-side bounded wait: one thread polls *flag (device memory) until it
+ * equals `expect`; after limit_ns nanoseconds it stores NBG_ERR_TIMEOUT in
+ * *status (device memory) and returns, leaving the context usable. */
+int nbg_wait_flag(const int *flag, int expect, uint64_t limit_ns, int *status, void *stream);
 
 /* -------------------------------------------------------------- assembly */
 /* Element stiffness and load of every element in nbots' operation order
@@ -132,9 +136,10 @@ int nbg_cg_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
  * (two rows per node with the same (2w, 2w+1) column pairs, sparse.c:36-52):
  * entry (slice s, k, lane r) sits at (slice_off[s] + k) * 32 + r; b64 holds
  * 4 doubles (a00 a01 a10 a11) per entry, b32 the same rounded to float and
- * blo the bfloat16 rounding of the remainders (double - float), so that
- * b32 + blo carries about 32 significant bits; dinv = 1 / diagonal per
- * scalar row.  Any array may be NULL when a caller does not need it. */
+ * blo the remainders (double - float) as signed 16-bit counts of
+ * 2^-16 ulp(float), so that b32 + blo carries about 40 significant bits in
+ * 6 bytes; dinv = 1 / diagonal per scalar row.  Any array may be NULL when a
+ * caller does not need it. */
 typedef struct {
     uint32_t N;            /* scalar rows (= 2 Nn) */
     uint32_t Nn;           /* node rows */
@@ -144,7 +149,7 @@ typedef struct {
     const uint32_t *bcol;
     const double *b64;
     const float *b32;
-    const uint16_t *blo;   /* 4 bfloat16 per entry */
+    const uint16_t *blo;   /* 4 remainder counts per entry */
     const double *dinv64;
     const float *dinv32;
 } nbg_bsr_t;
@@ -158,6 +163,15 @@ int nbg_bsr_fill(const nbg_bsr_t *A, const uint32_t *row_ptr, const uint32_t *co
                  const double *val, void *stream);
 int nbg_spmv_bsr_f64(const nbg_bsr_t *A, const double *x, double *y, void *stream);
 int nbg_spmv_bsr_f32(const nbg_bsr_t *A, const float *x, float *y, void *stream);
+/* Streamed SpMVs: each warp moves its slices of the matrix into shared
+ * memory with cp.async.bulk (double-buffered, mbarrier completion).
+ * _split: y = (b32 + blo)(xh + xl) with error-free FP32 arithmetic, y as
+ * yh (FP32) + yl (bfloat16 bits); the operator of nbg_cg_mixed.
+ * status: one device int, NBG_ERR_TIMEOUT if a copy never completed. */
+int nbg_spmv_bsr_split(const nbg_bsr_t *A, const float *xh, const uint16_t *xl, float *yh,
+                       uint16_t *yl, int *status, void *stream);
+int nbg_spmv_bsr_f64_stream(const nbg_bsr_t *A, const double *x, double *y, int *status,
+                            void *stream);
 
 /* Fast persistent FP64 Jacobi-PCG on the block layout: FMA arithmetic,
  * reciprocal diagonal, stop on the current ||g|| (not nbots' lagged one);
@@ -196,7 +210,8 @@ int nbg_cg_mixed(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_it
 #define NBG_METHOD_NBOTS 0   /* nbots' iteration in FP64 (nbg_cg_f64) */
 #define NBG_METHOD_FP64 1    /* fast FP64 on the block layout (nbg_cg_bsr_f64) */
 #define NBG_METHOD_MIXED 2   /* mixed precision, FP64 reliable updates (nbg_cg_mixed) */
-#define NBG_PATTERN_SAME 1u
+#define NBG_PATTERN_SAME 1u  /* same pattern as the previous call: send values only */
+#define NBG_CSR_ONLY 2u      /* skip the block layout (only NBG_METHOD_NBOTS will run) */
 
 typedef struct {
     uint32_t niter;

@@ -67,6 +67,7 @@ SIGS = {
     "nbg_h2d": ([vp, vp, sz, vp], i32),
     "nbg_d2h": ([vp, vp, sz, vp], i32),
     "nbg_stream_sync": ([vp], i32),
+    "nbg_wait_flag": ([vp, i32, u64, vp, vp], i32),
     "nbg_element_stiffness_f64": ([u32, u32, vp, vp, vp, f64, f64, f64, i32, f64, f64, vp, vp,
                                    vp, vp, vp], i32),
     "nbg_gather_assemble_f64": ([u32, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
@@ -83,6 +84,8 @@ SIGS = {
     "nbg_bsr_fill": ([C.POINTER(Bsr), vp, vp, vp, vp], i32),
     "nbg_spmv_bsr_f64": ([C.POINTER(Bsr), vp, vp, vp], i32),
     "nbg_spmv_bsr_f32": ([C.POINTER(Bsr), vp, vp, vp], i32),
+    "nbg_spmv_bsr_split": ([C.POINTER(Bsr), vp, vp, vp, vp, vp, vp], i32),
+    "nbg_spmv_bsr_f64_stream": ([C.POINTER(Bsr), vp, vp, vp, vp], i32),
     "nbg_cg_bsr_workspace_bytes": ([u32], sz),
     "nbg_cg_bsr_f64": ([C.POINTER(Bsr), vp, vp, u32, f64, C.c_uint, C.POINTER(CgResult), vp,
                         sz, vp], i32),

@@ -55,15 +55,14 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
         const float h00 = (float)a00, h01 = (float)a01, h10 = (float)a10, h11 = (float)a11;
         if (b32) reinterpret_cast<float4*>(b32)[e] = make_float4(h00, h01, h10, h11);
         if (blo) {
-            // remainders are exact in FP64; bfloat16 keeps FP32's exponent
-            // range, so they do not underflow as FP16 would
-            const __nv_bfloat162 l0 = __floats2bfloat162_rn((float)(a00 - (double)h00),
-                                                            (float)(a01 - (double)h01));
-            const __nv_bfloat162 l1 = __floats2bfloat162_rn((float)(a10 - (double)h10),
-                                                            (float)(a11 - (double)h11));
+            // remainders (exact in FP64) as 16-bit counts of 2^-16 ulp(hi)
+            const uint16_t q0 = (uint16_t)ulp16_encode(a00, h00);
+            const uint16_t q1 = (uint16_t)ulp16_encode(a01, h01);
+            const uint16_t q2 = (uint16_t)ulp16_encode(a10, h10);
+            const uint16_t q3 = (uint16_t)ulp16_encode(a11, h11);
             uint2 packed;
-            packed.x = *reinterpret_cast<const uint32_t*>(&l0);
-            packed.y = *reinterpret_cast<const uint32_t*>(&l1);
+            packed.x = (uint32_t)q0 | ((uint32_t)q1 << 16);
+            packed.y = (uint32_t)q2 | ((uint32_t)q3 << 16);
             reinterpret_cast<uint2*>(blo)[e] = packed;
         }
     }

@@ -68,3 +68,27 @@ extern "C" int nbg_host_free(void* ptr) {
     if (ptr) NBG_CHECK(cudaFreeHost(ptr));
     return NBG_OK;
 }
+
+namespace {
+// One thread waits until *flag == expect or `limit_ns` has passed; on expiry
+// it records NBG_ERR_TIMEOUT in *status and returns.  The same bounded wait
+// guards every grid barrier of the persistent solvers.
+__global__ void k_wait_flag(const int* flag, int expect, uint64_t limit_ns, int* status) {
+    const uint64_t t0 = nbg::globaltimer();
+    while (nbg::ld_volatile(flag) != expect) {
+        if (nbg::globaltimer() - t0 > limit_ns) {
+            atomicCAS(status, 0, NBG_ERR_TIMEOUT);
+            return;
+        }
+        __nanosleep(1000);
+    }
+}
+}  // namespace
+
+extern "C" int nbg_wait_flag(const int* flag, int expect, uint64_t limit_ns, int* status,
+                             void* stream) {
+    if (!flag || !status) return NBG_ERR_ARG;
+    k_wait_flag<<<1, 1, 0, (cudaStream_t)stream>>>(flag, expect, limit_ns, status);
+    NBG_CHECK(cudaGetLastError());
+    return NBG_OK;
+}

@@ -30,7 +30,7 @@ struct CgBsrArgs {
     unsigned flags;
 };
 
-__global__ void __launch_bounds__(kPersistThreads) k_cg_bsr_f64(CgBsrArgs a) {
+__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f64(CgBsrArgs a) {
     __shared__ double red[3 * 32];
     __shared__ double bc[3];
     const unsigned G = gridDim.x;

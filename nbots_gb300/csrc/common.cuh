@@ -176,6 +176,35 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
     return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
+// Remainder of an FP32 rounding stored as a 16-bit integer count of
+// 2^-16 ulp(hi): hi + lo then carries about 40 significant bits in 6 bytes.
+// The unit 2^(E - 166) (E = biased exponent of hi) is built from bits; for
+// |hi| < 2^-87 the remainder is dropped.
+__device__ __forceinline__ float ulp16_unit(float hi) {
+    const int E = (int)((__float_as_uint(hi) >> 23) & 0xffu);
+    return E >= 40 ? __uint_as_float((uint32_t)(E - 39) << 23) : 0.f;
+}
+
+__device__ __forceinline__ int16_t ulp16_encode(double a, float hi) {
+    const float unit = ulp16_unit(hi);
+    if (unit == 0.f) return 0;
+    double q = rint((a - (double)hi) / (double)unit);
+    q = q > 32767.0 ? 32767.0 : (q < -32767.0 ? -32767.0 : q);
+    return (int16_t)q;
+}
+
+__device__ __forceinline__ float ulp16_decode(int16_t q, float hi) {
+    return (float)q * ulp16_unit(hi);
+}
+
+// The four remainders of one 2x2 block (packed 16-bit counts) as floats.
+__device__ __forceinline__ float4 ulp16_decode4(uint2 v, float4 hi) {
+    return make_float4(ulp16_decode((int16_t)(v.x & 0xffffu), hi.x),
+                       ulp16_decode((int16_t)(v.x >> 16), hi.y),
+                       ulp16_decode((int16_t)(v.y & 0xffffu), hi.z),
+                       ulp16_decode((int16_t)(v.y >> 16), hi.w));
+}
+
 // a * b, both float-float
 __device__ __forceinline__ FF ff_mul(FF a, FF b) {
     FF p = two_prod(a.hi, b.hi);

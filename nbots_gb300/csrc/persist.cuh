@@ -9,7 +9,15 @@
 
 namespace nbg {
 
-constexpr int kPersistThreads = 256;
+// Launch shape of the persistent solvers (overridable at build time for tuning).
+#ifndef NBG_PERSIST_THREADS
+#define NBG_PERSIST_THREADS 512
+#endif
+#ifndef NBG_PERSIST_MIN_BLOCKS
+#define NBG_PERSIST_MIN_BLOCKS 2  // 64 registers per thread: 32 warps per SM
+#endif
+constexpr int kPersistThreads = NBG_PERSIST_THREADS;
+constexpr int kPersistMinBlocks = NBG_PERSIST_MIN_BLOCKS;
 constexpr unsigned kMaxBlocks = 4096;
 
 inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
@@ -108,6 +116,42 @@ inline int coop_grid(const void* fn, uint32_t n_slices, unsigned* G) {
     if (g > kMaxBlocks) g = kMaxBlocks;
     *G = g;
     return NBG_OK;
+}
+
+// Grid of a persistent kernel whose blocks keep `bytes_per_slice` of own-row
+// data per slice in dynamic shared memory: the largest blocks-per-SM count
+// (kPersistMinBlocks, then 1) at which every block's slices fit.  *dyn = 0
+// means they do not fit even at one block per SM and the kernel must keep
+// those rows in global memory.
+inline int coop_grid_resident(const void* fn, uint32_t n_slices, size_t bytes_per_slice,
+                              unsigned* G, size_t* dyn) {
+    int dev = 0, nsm = 0, optin = 0;
+    NBG_CHECK(cudaGetDevice(&dev));
+    NBG_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    NBG_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    NBG_CHECK(cudaFuncGetAttributes(&fa, fn));
+    const unsigned want = (n_slices + kPersistThreads / 32 - 1) / (kPersistThreads / 32);
+    for (int per_sm = kPersistMinBlocks; bytes_per_slice && per_sm >= 1; --per_sm) {
+        unsigned g = (unsigned)nsm * (unsigned)per_sm;
+        if (want < g) g = want;
+        if (g < 1) g = 1;
+        const size_t spb = (n_slices + g - 1) / g;
+        const size_t bytes = spb * bytes_per_slice;
+        if (bytes + fa.sharedSizeBytes > (size_t)optin) continue;
+        NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                       (int)bytes));
+        int occ = 0;
+        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, bytes));
+        if ((unsigned)occ * (unsigned)nsm >= g) {
+            *G = g;
+            *dyn = bytes;
+            return NBG_OK;
+        }
+    }
+    *dyn = 0;
+    NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 0));
+    return coop_grid(fn, n_slices, G);
 }
 
 }  // namespace nbg

@@ -1,0 +1,264 @@
+/*
+ * Drop-in nb_fem_compute_2D_Solid_Mechanics / nb_fem_compute_stress_from_strain
+ * (nbots_dropin.h) on the device FEM system (fem.c).
+ *
+ * The mesh, boundary conditions, material and element type are read through
+ * nbots' public accessors only, so the function works on nbots' own objects
+ * when linked ahead of libnbots.so, and on libnbots_host.so's otherwise.
+ * Function-valued conditions are evaluated here, at the points where nbots
+ * evaluates them (set_bconditions.c:63-260): segment nodes, vertex nodes for
+ * Dirichlet, and (0,0) for Neumann vertex loads.
+ */
+#include <stdlib.h>
+#include <string.h>
+
+#include "nbots_dropin.h"
+#include "nbots_gb300.h"
+
+typedef struct {
+	nbg_mesh_t m;
+	double *nod;
+	uint32_t *conn, *edg, *vtx, *sgm_ptr, *sgm_nodes;
+	uint32_t N_sgm;
+	nbg_bc_t *bc;
+	double **vals;
+	uint32_t N_bc;
+} host_problem_t;
+
+static void free_problem(host_problem_t *h)
+{
+	free(h->nod);
+	free(h->conn);
+	free(h->edg);
+	free(h->vtx);
+	free(h->sgm_ptr);
+	free(h->sgm_nodes);
+	for (uint32_t k = 0; k < h->N_bc; k++)
+		free(h->vals ? h->vals[k] : NULL);
+	free(h->vals);
+	free(h->bc);
+}
+
+static int read_mesh(const nb_mesh2D_t *part, uint32_t nen, host_problem_t *h)
+{
+	const uint32_t Nn = nb_mesh2D_get_N_nodes(part), Ne = nb_mesh2D_get_N_elems(part);
+	const uint32_t Nd = nb_mesh2D_get_N_edges(part);
+	h->nod = malloc(16 * (size_t)(Nn ? Nn : 1));
+	h->conn = malloc(4 * (size_t)nen * (Ne ? Ne : 1));
+	h->edg = malloc(8 * (size_t)(Nd ? Nd : 1));
+	if (!h->nod || !h->conn || !h->edg)
+		return NBG_ERR_NOMEM;
+	for (uint32_t i = 0; i < Nn; i++) {
+		h->nod[2 * i] = nb_mesh2D_node_get_x(part, i);
+		h->nod[2 * i + 1] = nb_mesh2D_node_get_y(part, i);
+	}
+	for (uint32_t e = 0; e < Ne; e++)
+		for (uint32_t k = 0; k < nen; k++)
+			h->conn[e * nen + k] = nb_mesh2D_elem_get_adj(part, e, (uint8_t)k);
+	for (uint32_t i = 0; i < Nd; i++) {
+		h->edg[2 * i] = nb_mesh2D_edge_get_1n(part, i);
+		h->edg[2 * i + 1] = nb_mesh2D_edge_get_2n(part, i);
+	}
+	h->m = (nbg_mesh_t){nen, Nn, Ne, Nd, h->nod, h->conn, h->edg};
+	const uint32_t Nv = nb_mesh2D_get_N_invtx(part), Ns = nb_mesh2D_get_N_insgm(part);
+	h->vtx = malloc(4 * (size_t)(Nv ? Nv : 1));
+	h->sgm_ptr = malloc(4 * ((size_t)Ns + 1));
+	if (!h->vtx || !h->sgm_ptr)
+		return NBG_ERR_NOMEM;
+	for (uint32_t i = 0; i < Nv; i++)
+		h->vtx[i] = nb_mesh2D_get_invtx(part, i);
+	h->sgm_ptr[0] = 0;
+	for (uint32_t s = 0; s < Ns; s++)
+		h->sgm_ptr[s + 1] = h->sgm_ptr[s] + nb_mesh2D_insgm_get_N_nodes(part, s);
+	h->sgm_nodes = malloc(4 * (size_t)(h->sgm_ptr[Ns] ? h->sgm_ptr[Ns] : 1));
+	if (!h->sgm_nodes)
+		return NBG_ERR_NOMEM;
+	for (uint32_t s = 0; s < Ns; s++)
+		for (uint32_t i = 0; i < h->sgm_ptr[s + 1] - h->sgm_ptr[s]; i++)
+			h->sgm_nodes[h->sgm_ptr[s] + i] = nb_mesh2D_insgm_get_node(part, s, i);
+	h->N_sgm = Ns;
+	return NBG_OK;
+}
+
+static int read_bcond(const nb_mesh2D_t *part, const nb_bcond_t *bcond, host_problem_t *h)
+{
+	static const int cat[4][2] = {{NB_DIRICHLET, NB_BC_ON_POINT}, {NB_NEUMANN, NB_BC_ON_POINT},
+				      {NB_DIRICHLET, NB_BC_ON_SEGMENT},
+				      {NB_NEUMANN, NB_BC_ON_SEGMENT}};
+	if (nb_bcond_get_N_dof(bcond) != 2)
+		return NBG_ERR_ARG;
+	void *it = malloc(nb_bcond_iter_get_memsize());
+	if (!it)
+		return NBG_ERR_NOMEM;
+	uint32_t cap = 0;
+	for (int pass = 0; pass < 2; pass++) {
+		uint32_t n = 0;
+		for (int c = 0; c < 4; c++) {
+			nb_bcond_iter_init(it);
+			nb_bcond_iter_set_conditions(it, bcond, (nb_bcond_id)cat[c][0],
+						     (nb_bcond_where)cat[c][1]);
+			while (nb_bcond_iter_has_more(it)) {
+				nb_bcond_iter_go_next(it);
+				if (pass == 1) {
+					nbg_bc_t *b = &h->bc[n];
+					memset(b, 0, sizeof(*b));
+					b->kind = cat[c][0] == NB_DIRICHLET ? 0u : 1u;
+					b->where = cat[c][1] == NB_BC_ON_POINT ? 0u : 1u;
+					b->id = nb_bcond_iter_get_id(it);
+					b->mask[0] = nb_bcond_iter_get_mask(it, 0);
+					b->mask[1] = nb_bcond_iter_get_mask(it, 1);
+					double x0[2] = {0.0, 0.0};
+					if (!nb_bcond_iter_val_is_function(it)) {
+						nb_bcond_iter_get_val(it, 2, x0, 0.0, b->val);
+					} else {
+						uint32_t nv = 1;
+						if (b->where == 1) {
+							if (b->id >= h->N_sgm) {
+								free(it);
+								return NBG_ERR_ARG;
+							}
+							nv = h->sgm_ptr[b->id + 1] - h->sgm_ptr[b->id];
+						}
+						double *v = malloc(16 * (size_t)nv);
+						if (!v) {
+							free(it);
+							return NBG_ERR_NOMEM;
+						}
+						h->vals[n] = v;
+						for (uint32_t i = 0; i < nv; i++) {
+							double x[2] = {0.0, 0.0};
+							if (!(b->kind == 1 && b->where == 0)) {
+								uint32_t nid = b->where == 1 ?
+									h->sgm_nodes[h->sgm_ptr[b->id] + i] :
+									h->vtx[b->id];
+								x[0] = h->nod[2 * nid];
+								x[1] = h->nod[2 * nid + 1];
+							}
+							nb_bcond_iter_get_val(it, 2, x, 0.0, v + 2 * i);
+						}
+						b->n_nv = nv;
+						b->node_vals = v;
+					}
+				}
+				n++;
+			}
+			nb_bcond_iter_finish(it);
+		}
+		if (pass == 0) {
+			cap = n;
+			h->bc = calloc(cap ? cap : 1, sizeof(nbg_bc_t));
+			h->vals = calloc(cap ? cap : 1, sizeof(double *));
+			if (!h->bc || !h->vals) {
+				free(it);
+				return NBG_ERR_NOMEM;
+			}
+			h->N_bc = cap;
+		}
+	}
+	free(it);
+	return NBG_OK;
+}
+
+int nb_fem_compute_2D_Solid_Mechanics(const nb_mesh2D_t *part, const nb_fem_elem_t *elemtype,
+				      const nb_material_t *material, const nb_bcond_t *bcond,
+				      bool enable_self_weight, double gravity[2],
+				      nb_analysis2D_t analysis2D, nb_analysis2D_params *params2D,
+				      const bool *elements_enabled, double *displacement,
+				      double *strain)
+{
+	(void)analysis2D;
+	const uint32_t nen = nb_fem_elem_get_N_nodes(elemtype);
+	if (nen != 3 && nen != 4)
+		return NBG_ERR_ARG;
+	host_problem_t h;
+	memset(&h, 0, sizeof(h));
+	double *E = NULL;
+	uint8_t *en = NULL;
+	nbg_fem_t *f = NULL;
+	int rc = read_mesh(part, nen, &h);
+	if (rc == NBG_OK)
+		rc = read_bcond(part, bcond, &h);
+	const uint32_t Ne = h.m.N_elem;
+	if (rc == NBG_OK) {
+		E = malloc(8 * (size_t)(Ne ? Ne : 1));
+		if (!E)
+			rc = NBG_ERR_NOMEM;
+		for (uint32_t e = 0; E && e < Ne; e++)
+			E[e] = nb_material_get_elasticity_module(material);
+	}
+	if (rc == NBG_OK && elements_enabled) {
+		en = malloc(Ne ? Ne : 1);
+		if (!en)
+			rc = NBG_ERR_NOMEM;
+		for (uint32_t e = 0; en && e < Ne; e++)
+			en[e] = elements_enabled[e] ? 1 : 0;
+	}
+	if (rc == NBG_OK)
+		rc = nbg_fem_create(&f, &h.m, NULL);
+	if (rc == NBG_OK) {
+		double g2[2] = {gravity ? gravity[0] : 0.0, gravity ? gravity[1] : 0.0};
+		rc = nbg_fem_assemble(f, E, nb_material_get_poisson_module(material),
+				      params2D->thickness, nb_material_get_density(material),
+				      enable_self_weight, g2, en);
+	}
+	if (rc == NBG_OK) {
+		nbg_bcs_t b = {h.vtx, h.N_sgm, h.sgm_ptr, h.sgm_nodes, h.N_bc, h.bc};
+		rc = nbg_fem_apply_bcs(f, &b, 1.0);
+	}
+	if (rc == NBG_OK) {
+		/* solver() of static_elasticity2D.c:83-97: x0 = 0, max_iter = N,
+		 * tol 1e-8 absolute; "not converged" counts as success */
+		nbg_cg_result_t r;
+		int st = nbg_fem_solve(f, nbg_fem_n_dof(f), 1e-8, NBG_CG_JACOBI, &r);
+		rc = st < 0 ? st : NBG_OK;
+	}
+	if (rc == NBG_OK)
+		rc = nbg_fem_strain(f);
+	if (rc == NBG_OK)
+		rc = nbg_fem_download(f, NBG_FEM_U, displacement);
+	if (rc == NBG_OK)
+		rc = nbg_fem_download(f, NBG_FEM_STRAIN, strain);
+	nbg_fem_destroy(f);
+	free(E);
+	free(en);
+	free_problem(&h);
+	return rc;
+}
+
+void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t *elemtype,
+				       const nb_material_t *material, nb_analysis2D_t analysis2D,
+				       double *strain, const bool *elements_enabled,
+				       double *stress)
+{
+	(void)analysis2D;
+	const uint32_t nen = nb_fem_elem_get_N_nodes(elemtype);
+	const size_t ng = nen == 4 ? 4 : 1;
+	const size_t n3 = 3 * ng * N_elements;
+	double *E = malloc(8 * (size_t)(N_elements ? N_elements : 1));
+	uint8_t *en = elements_enabled ? malloc(N_elements ? N_elements : 1) : NULL;
+	void *dE = NULL, *den = NULL, *ds = NULL, *dt = NULL;
+	int rc = E && (!elements_enabled || en) ? NBG_OK : NBG_ERR_NOMEM;
+	for (uint32_t e = 0; rc == NBG_OK && e < N_elements; e++) {
+		E[e] = nb_material_get_elasticity_module(material);
+		if (en)
+			en[e] = elements_enabled[e] ? 1 : 0;
+	}
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&dE, 8 * (size_t)(N_elements ? N_elements : 1));
+	if (rc == NBG_OK && en) rc = nbg_dev_alloc(&den, N_elements ? N_elements : 1);
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&ds, 8 * (n3 ? n3 : 1));
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&dt, 8 * (n3 ? n3 : 1));
+	if (rc == NBG_OK) rc = nbg_h2d(dE, E, 8 * (size_t)N_elements, NULL);
+	if (rc == NBG_OK && en) rc = nbg_h2d(den, en, N_elements, NULL);
+	if (rc == NBG_OK) rc = nbg_h2d(ds, strain, 8 * n3, NULL);
+	if (rc == NBG_OK)
+		rc = nbg_stress_f64(nen, N_elements, dE, nb_material_get_poisson_module(material),
+				    den, ds, dt, NULL);
+	if (rc == NBG_OK) rc = nbg_d2h(stress, dt, 8 * n3, NULL);
+	if (rc == NBG_OK) rc = nbg_stream_sync(NULL);
+	nbg_dev_free(dE);
+	nbg_dev_free(den);
+	nbg_dev_free(ds);
+	nbg_dev_free(dt);
+	free(E);
+	free(en);
+}

@@ -78,7 +78,8 @@ int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
 		uint32_t *so = malloc(((size_t)S + 1) * sizeof(uint32_t));
 		if (!so)
 			TRY(NBG_ERR_NOMEM);
-		s->bsr_ok = N > 0 && nbg_bsr_plan(N, row_ptr, col_idx, so) == NBG_OK;
+		s->bsr_ok = N > 0 && !(flags & NBG_CSR_ONLY) &&
+			    nbg_bsr_plan(N, row_ptr, col_idx, so) == NBG_OK;
 		if (s->bsr_ok) {
 			const uint64_t ent = 32ull * so[S];
 			int r2 = nbg_dev_alloc((void **)&s->slice_off, 4 * ((size_t)S + 1));

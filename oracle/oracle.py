@@ -59,6 +59,8 @@ def lib():
         L.orc_assemble.argtypes = [vp, vp, vp, vp, f64, f64, f64, i32, vp, vp, vp, vp]
         L.orc_element.argtypes = [vp, u32, f64, f64, f64, f64, i32, vp, i32, vp, vp]
         L.orc_set_bconditions.argtypes = [vp, vp, vp, vp, vp, vp, f64]
+        L.orc_set_dirichlet.argtypes = [vp, vp, vp, vp, u32, f64]
+        L.orc_set_dirichlet.restype = None
         L.orc_spmv.argtypes = [u32, vp, vp, vp, vp, vp, i32]
         L.orc_spmv.restype = None
         L.orc_cg_jacobi.argtypes = [u32, vp, vp, vp, vp, vp, u32, f64, vp, vp, i32]

@@ -1,0 +1,106 @@
+"""nbots' own entry points, called as an nbots program calls them, on the
+GPU drop-in: SpMV bit-exact, CG within 1e-10 relative L2 of nbots' answer,
+the FEM entry on nbots-interface objects, and nbots' known answers."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_CASES, load_golden
+from kat import BEAM_MAX_DISP, PWH_MAX_VM_ERR, max_disp, pwh_mean_vm_error
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+FEM_CASES = [c for c in GOLDEN_CASES if c != "q4_lognormal_32x16"]  # one material only
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def G():
+    from nbots_gb300 import _lib as L
+    from nbots_gb300.dropin import libs
+    assert L.lib().nbg_device_count() > 0
+    return libs()[0]
+
+
+@pytest.mark.parametrize("name", ["c1_q4_64x32", "t3_beam_cantilever", "q4_allbc_16x8"])
+def test_multiply_vector_bit_exact(G, name):
+    from nbots_gb300.dropin import sparse_from_csr
+    p, d = load_golden(name)
+    A, keep = sparse_from_csr(p, d["K_bc"])
+    y = np.zeros(p.n_dof)
+    x = np.ascontiguousarray(d["spmv_x"])
+    G.nb_sparse_multiply_vector(A, x.ctypes.data, y.ctypes.data, 4)
+    assert np.array_equal(y.view(np.uint64), d["spmv_y"].view(np.uint64))
+    G.nb_sparse_destroy(A)
+
+
+@pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if c != "q4_distorted_8x4"])
+def test_cg_precond_jacobi(G, name):
+    from nbots_gb300.dropin import sparse_from_csr
+    p, d = load_golden(name)
+    A, keep = sparse_from_csr(p, d["K_bc"])
+    b = np.ascontiguousarray(d["F_bc"])
+    x = np.zeros(p.n_dof)
+    it, tr = C.c_uint32(0), C.c_double(0)
+    st = G.nb_sparse_solve_CG_precond_Jacobi(A, b.ctypes.data, x.ctypes.data, p.n_dof, 1e-8,
+                                              C.byref(it), C.byref(tr), 1)
+    ref_it = int(d["cg_niter"][0])
+    assert st == int(d["cg_status"][0])
+    assert abs(it.value - ref_it) <= max(2, ref_it // 10)
+    assert rel(x, d["u"]) < 1e-10
+    # the not-converged return path (max_iter = 7)
+    x7 = np.zeros(p.n_dof)
+    st7 = G.nb_sparse_solve_CG_precond_Jacobi(A, b.ctypes.data, x7.ctypes.data, 7, 1e-8,
+                                               C.byref(it), C.byref(tr), 1)
+    assert (st7, it.value) == (1, 7) and rel(x7, d["u_it7"]) < 1e-12
+    G.nb_sparse_destroy(A)
+
+
+def test_plain_cg_matches_oracle(G):
+    from nbots_gb300.dropin import sparse_from_csr
+    p, d = load_golden("q4_allbc_16x8")
+    A, keep = sparse_from_csr(p, d["K_bc"])
+    b = np.ascontiguousarray(d["F_bc"])
+    x = np.zeros(p.n_dof)
+    it, tr = C.c_uint32(0), C.c_double(0)
+    st = G.nb_sparse_solve_conjugate_gradient(A, b.ctypes.data, x.ctypes.data, 4 * p.n_dof,
+                                               1e-8, C.byref(it), C.byref(tr), 1)
+    u, oit, otr, ost = O.cg_jacobi(d["row_ptr"], d["col_idx"], d["K_bc"], b,
+                                   max_iter=4 * p.n_dof, plain=True)
+    assert st == ost and abs(it.value - oit) <= max(2, oit // 10)
+    assert rel(x, u) < 1e-10
+    G.nb_sparse_destroy(A)
+
+
+@pytest.mark.parametrize("name", FEM_CASES)
+def test_fem_entry(G, name):
+    from nbots_gb300.dropin import NbotsObjects
+    p, d = load_golden(name)
+    ob = NbotsObjects(p)
+    st, u, strain = ob.fem()
+    if int(d["assemble_status"][0]):
+        assert st == 1          # distorted element, like nbots
+        return
+    assert st == 0
+    assert rel(u, d["fem_u"]) < 1e-10
+    assert rel(strain, d["fem_strain"]) < 1e-8
+    # stress from nbots' own strain is bit-exact
+    s = ob.stress(d["fem_strain"])
+    assert np.array_equal(s.view(np.uint64), d["fem_stress"].view(np.uint64))
+    ob.close()
+
+
+def test_fem_entry_known_answers(G):
+    from nbots_gb300.dropin import NbotsObjects
+    p, _ = load_golden("t3_beam_cantilever")
+    ob = NbotsObjects(p)
+    st, u, _ = ob.fem()
+    assert st == 0 and abs(max_disp(u) - BEAM_MAX_DISP) < 1e-6
+    p, _ = load_golden("t3_plate_with_hole")
+    ob = NbotsObjects(p)
+    st, u, strain = ob.fem()
+    assert st == 0 and pwh_mean_vm_error(p, ob.stress(strain)) < PWH_MAX_VM_ERR

@@ -1,0 +1,151 @@
+"""Fast FP64 and mixed-precision solvers, the host-buffer C ABI, and the
+failure paths, on the GPU.
+
+Tolerances: both fast solvers stop on the relative residual they are given;
+their true FP64 residual (checked here with the oracle's SpMV) must meet it.
+Displacements are compared with nbots' own result (reference fixture) and
+with an oracle solution converged to relres 1e-13: the mixed solver at
+tol 1e-11 must agree with it to 1e-8 relative L2."""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from conftest import load_golden
+from kat import BEAM_MAX_DISP, max_disp
+from oracle import oracle as O
+
+pytestmark = pytest.mark.gpu
+Q4_CASES = ["c1_q4_64x32", "q4_lognormal_32x16", "q4_allbc_16x8"]
+
+
+def rel(a, b):
+    return float(np.linalg.norm(a - b) / np.linalg.norm(b))
+
+
+@pytest.fixture(scope="module")
+def L():
+    from nbots_gb300 import _lib
+    assert _lib.lib().nbg_device_count() > 0
+    return _lib
+
+
+def system(name):
+    from nbots_gb300.fem import FemSystem
+    p, d = load_golden(name)
+    s = FemSystem(p)
+    assert s.assemble() == 0
+    s.apply_bcs()
+    return p, d, s
+
+
+def true_relres(d, u):
+    r = d["F_bc"] - O.spmv(d["row_ptr"], d["col_idx"], d["K_bc"], u)
+    return float(np.linalg.norm(r) / np.linalg.norm(d["F_bc"]))
+
+
+def tight(d):
+    u, _, _, _ = O.cg_jacobi(d["row_ptr"], d["col_idx"], d["K_bc"], d["F_bc"],
+                             max_iter=20 * d["F_bc"].shape[0],
+                             tol=1e-13 * np.linalg.norm(d["F_bc"]))
+    return u
+
+
+@pytest.mark.parametrize("name", Q4_CASES + ["t3_beam_cantilever"])
+def test_fast_fp64_solver(L, name):
+    p, d, s = system(name)
+    r = s.solve_fast(tol=1e-10)
+    u = s.get(L.FEM_U)
+    assert r.status == 0
+    assert true_relres(d, u) <= 1.05e-10
+    assert rel(u, tight(d)) < 1e-8
+
+
+@pytest.mark.parametrize("name", Q4_CASES + ["t3_beam_cantilever"])
+def test_mixed_solver(L, name):
+    p, d, s = system(name)
+    r = s.solve_mixed(tol=1e-8)
+    u = s.get(L.FEM_U)
+    assert r.status == 0 and r.relres <= 1e-8
+    assert true_relres(d, u) <= 1.05e-8
+    # both nbots' answer and this one stop near relres 1e-8
+    assert rel(u, d["u"]) < 1e-5
+    r = s.solve_mixed(tol=1e-11)
+    u = s.get(L.FEM_U)
+    assert r.status == 0 and true_relres(d, u) <= 1.05e-11
+    assert rel(u, tight(d)) < 1e-8
+
+
+def test_mixed_known_answer_and_determinism(L):
+    p, d, s = system("t3_beam_cantilever")
+    s.solve_mixed(tol=1e-10)
+    u1 = s.get(L.FEM_U)
+    assert abs(max_disp(u1) - BEAM_MAX_DISP) < 1e-6
+    s.solve_mixed(tol=1e-10)
+    assert np.array_equal(s.get(L.FEM_U).view(np.uint64), u1.view(np.uint64))
+
+
+@pytest.mark.parametrize("method", [0, 1, 2])
+def test_host_buffer_solver(L, method):
+    lib = L.lib()
+    p, d = load_golden("c1_q4_64x32")
+    N = d["F_bc"].shape[0]
+    h = C.c_void_p()
+    assert lib.nbg_solver_create(C.byref(h), None) == 0
+    rp, ci, K, F = (np.ascontiguousarray(d[k]) for k in ("row_ptr", "col_idx", "K_bc", "F_bc"))
+    for flags in (0, L.PATTERN_SAME):
+        assert lib.nbg_solver_set_matrix(h, N, rp.ctypes.data, ci.ctypes.data, K.ctypes.data,
+                                         flags) == 0
+        x = np.zeros(N)
+        info = L.SolveInfo()
+        tol = 1e-8 if method == 0 else 1e-10
+        fl = L.CG_JACOBI | (0 if method == 0 else L.CG_RELATIVE)
+        rc = lib.nbg_solver_solve(h, F.ctypes.data, x.ctypes.data, N * 4, tol, fl, method,
+                                  C.byref(info))
+        assert rc == 0 and info.status == 0
+        if method == 0:
+            # nbots' iteration, absolute tolerance: the reference's answer
+            assert rel(x, d["u"]) < 1e-10
+        else:
+            assert true_relres(d, x) <= 1.05e-10
+    lib.nbg_solver_destroy(h)
+
+
+def test_missing_pattern_pair_is_an_error(L):
+    """nbots exits when an element pair is not in the pattern
+    (sparse.c:213-218); here assembly returns NBG_ERR_PATTERN."""
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.fem import FemSystem
+    p = W.cantilever_q4(8, 4)
+    p.edges = p.edges[1:]          # drop one mesh edge
+    s = FemSystem(p)
+    assert s.assemble() == -5
+
+
+def test_not_spd_does_not_hang(L):
+    """A negative modulus makes K indefinite: the solvers must come back with
+    a status, never hang."""
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.fem import FemSystem
+    p = W.cantilever_q4(16, 8)
+    p.E[::3] = -1.0
+    s = FemSystem(p)
+    assert s.assemble() == 0
+    s.apply_bcs()
+    r = s.solve(max_iter=500)
+    assert r.status in (0, 1)
+    r2 = s.solve_mixed(max_iter=500)
+    assert r2.status in (0, 1)
+
+
+def test_bounded_device_wait_times_out_and_context_survives(L):
+    from nbots_gb300.device import DeviceArray
+    lib = L.lib()
+    flag = DeviceArray(np.zeros(1, np.int32))
+    status = DeviceArray(np.zeros(1, np.int32))
+    assert lib.nbg_wait_flag(flag.ptr, 1, 50_000_000, status.ptr, None) == 0
+    assert lib.nbg_stream_sync(None) == 0
+    assert int(status.numpy()[0]) == -2       # NBG_ERR_TIMEOUT
+    # the context is still usable
+    p, d, s = system("q4_allbc_16x8")
+    assert s.solve().status == 0
