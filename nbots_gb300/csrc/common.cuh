@@ -61,11 +61,15 @@ __device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, int
     if (threadIdx.x == 0) {
         int stop = 0;
         unsigned gen = ld_acquire(&bar[1]);
-        __threadfence();
-        unsigned prev = atomicAdd(&bar[0], 1u);
+        // arrival: one acquire-release atomic publishes this block's writes
+        unsigned prev;
+        asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;"
+                     : "=r"(prev)
+                     : "l"(&bar[0])
+                     : "memory");
         if (prev == nblocks - 1) {
-            atomicExch(&bar[0], 0u);
-            __threadfence();
+            // nobody touches the count again before the generation moves
+            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&bar[0]) : "memory");
             st_release(&bar[1], gen + 1);
         } else {
             uint64_t t0 = globaltimer();

@@ -2,15 +2,15 @@
 //
 // GB300 runs FP32 at many times its FP64 rate, and the stiffness matrices
 // here have condition numbers near 1e8, where plain FP32 CG needs several
-// times more iterations than FP64.  Measured on the lognormal cantilever,
-// the inflation comes from three places: FP32 matrix values (the inner
-// operator then differs from the FP64 one behind the residual), FP32 search
+// times more iterations than FP64.  Measured on the lognormal cantilever
+// (1M dof), the inflation comes from three places: the precision of the
+// matrix values (even 32 significant bits cost 1.33x the iterations: the
+// inner operator must match the FP64 one behind the residual), FP32 search
 // directions p and FP32 products A p, and an FP32 correction x.  The FP32
 // residual r is harmless.  So the inner iteration runs on the FP32 pipes
 // with:
-//   matrix      FP32 hi + bfloat16 lo per value (about 32 significant bits,
-//               6 B/value instead of 8; bfloat16 keeps FP32's exponent
-//               range, FP16 would underflow the remainders),
+//   matrix      FP32 hi + a 16-bit remainder in units of 2^-16 ulp(hi)
+//               (about 40 significant bits in 6 B/value instead of 8),
 //   p, A p      FP32 hi + bfloat16 lo per dof,
 //   x           float-float (FP32 hi + FP32 lo),
 //   r           FP32,
@@ -21,7 +21,10 @@
 // values whenever |r| has fallen by `delta` since the last one; p is kept,
 // so the Krylov progress survives.  Convergence is judged on the FP64
 // residual only.  Three grid barriers per iteration (L1 | L2 | L3 of
-// cg_precond_jacobi.c:50-74).
+// cg_precond_jacobi.c:50-74): folding L3 into the next SpMV (each block
+// rebuilding z + beta p for the columns it reads) measured slower, 77 vs
+// 66 us per iteration at 1M dof, because the float-float rebuild per column
+// costs more issue slots and gather bytes than the barrier it saves.
 #include <cstdint>
 
 #include "persist.cuh"
