@@ -131,6 +131,21 @@ int nbg_cg_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
                double tol, unsigned flags, nbg_cg_result_t *result, void *ws,
                size_t ws_bytes, void *stream);
 
+/* nbg_cg_f64 without any device allocation, for callers that cannot
+ * allocate device memory while they solve (a host application that keeps
+ * the GPU's memory in its own pool and forbids libraries to call cudaMalloc,
+ * or a loop that cannot take the device-wide synchronisation of
+ * cudaMalloc / cudaFree).  No counterpart in nbots.  The scratch lives in a
+ * 16 MiB file-scope device array that every GPU loading this library holds
+ * until exit, so N is limited to 345,408 dofs (larger N: NBG_ERR_ARG, with
+ * the reason in nbg_last_error).  The first call on a device looks up the
+ * array's address with that device current; make it before any stream
+ * capture.  All calls share the array: calls that overlap on the GPU race
+ * and must be serialised by the caller. */
+int nbg_cg_f64_noalloc(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+                       const double *val, const double *b, double *x, uint32_t max_iter,
+                       double tol, unsigned flags, nbg_cg_result_t *result, void *stream);
+
 /* ------------------------------------------------- 2x2-block SELL layout */
 /* Device arrays of the node-block layout of a CSR from nb_sparse_create(.., 2)
  * (two rows per node with the same (2w, 2w+1) column pairs, sparse.c:36-52):

@@ -80,6 +80,8 @@ SIGS = {
     "nbg_cg_workspace_bytes": ([u32], sz),
     "nbg_cg_f64": ([u32, vp, vp, vp, vp, vp, u32, f64, C.c_uint, C.POINTER(CgResult), vp, sz,
                     vp], i32),
+    "nbg_cg_f64_noalloc": ([u32, vp, vp, vp, vp, vp, u32, f64, C.c_uint, C.POINTER(CgResult),
+                            vp], i32),
     "nbg_bsr_plan": ([u32, vp, vp, vp], i32),
     "nbg_bsr_fill": ([C.POINTER(Bsr), vp, vp, vp, vp], i32),
     "nbg_spmv_bsr_f64": ([C.POINTER(Bsr), vp, vp, vp], i32),

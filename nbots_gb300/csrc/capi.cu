@@ -15,6 +15,11 @@ int nbg_cuda_error(cudaError_t e) {
     return NBG_ERR_CUDA;
 }
 
+int nbg_error_text(int code, const char* text) {
+    std::snprintf(g_last_error, sizeof(g_last_error), "%s", text);
+    return code;
+}
+
 extern "C" const char* nbg_version(void) { return "nbots_gb300 0.1 (sm_103a)"; }
 
 extern "C" const char* nbg_last_error(void) { return g_last_error; }

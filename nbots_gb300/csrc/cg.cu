@@ -13,6 +13,8 @@
 // division by the diagonal); the dot products are block-tree plus a fixed
 // block order, identical from run to run.
 #include <cstdint>
+#include <cstdio>
+#include <mutex>
 
 #include "common.cuh"
 
@@ -297,4 +299,65 @@ extern "C" int nbg_cg_f64(uint32_t N, const uint32_t* row_ptr, const uint32_t* c
     }
     if (own) cudaFree(own);
     return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Allocation-free variant of nbg_cg_f64.
+//
+// Some callers cannot allocate device memory when they solve: a host
+// application that reserves the GPU's memory in its own pool and forbids
+// libraries to call cudaMalloc, or a loop that cannot take the device-wide
+// synchronisation cudaMalloc / cudaFree imply.  This entry point runs the
+// same kernel with its scratch (work vectors, partial sums, barrier and
+// status words) in a file-scope device array instead of a workspace.
+//
+// Limits and sharing:
+//  * the array holds kNoAllocScratchBytes (16 MiB) on every GPU that loads
+//    this library, until the process exits; a system fits when
+//    nbg_cg_workspace_bytes(N) is at most that, i.e. N <= 345,408 dofs;
+//    larger N is rejected with NBG_ERR_ARG and a message in nbg_last_error;
+//  * the array's device address is looked up (cudaGetSymbolAddress) by the
+//    first call on each device, with that device current; make that first
+//    call before any stream capture;
+//  * every call shares the array and it keeps the last call's contents: each
+//    call clears the barrier, status and result words it needs at zero, and
+//    the work vectors are written before they are read;
+//  * calls that overlap on the GPU (two streams, or two host threads on one
+//    device) race on the array and must be serialised by the caller.
+namespace {
+constexpr size_t kNoAllocScratchBytes = 16u << 20;
+constexpr int kNoAllocMaxDevices = 64;
+static __device__ __align__(256) unsigned char g_cg_scratch[kNoAllocScratchBytes];
+std::mutex g_noalloc_lock;
+void* g_noalloc_ptr[kNoAllocMaxDevices];
+}  // namespace
+
+extern "C" int nbg_cg_f64_noalloc(uint32_t N, const uint32_t* row_ptr, const uint32_t* col_idx,
+                                  const double* val, const double* b, double* x,
+                                  uint32_t max_iter, double tol, unsigned flags,
+                                  nbg_cg_result_t* result, void* stream) {
+    const size_t need = layout(N).total;
+    if (need > kNoAllocScratchBytes) {
+        char msg[200];
+        std::snprintf(msg, sizeof(msg),
+                      "nbg_cg_f64_noalloc: N = %u needs %zu bytes of scratch; the static "
+                      "array holds %zu (N <= 345408)",
+                      N, need, kNoAllocScratchBytes);
+        return nbg_error_text(NBG_ERR_ARG, msg);
+    }
+    int dev = 0;
+    NBG_CHECK(cudaGetDevice(&dev));
+    if (dev < 0 || dev >= kNoAllocMaxDevices) return NBG_ERR_ARG;
+    void* ptr = nullptr;
+    {
+        std::lock_guard<std::mutex> g(g_noalloc_lock);
+        if (!g_noalloc_ptr[dev]) {
+            void* p = nullptr;
+            NBG_CHECK(cudaGetSymbolAddress(&p, g_cg_scratch));
+            g_noalloc_ptr[dev] = p;
+        }
+        ptr = g_noalloc_ptr[dev];
+    }
+    return nbg_cg_f64(N, row_ptr, col_idx, val, b, x, max_iter, tol, flags, result, ptr,
+                      kNoAllocScratchBytes, stream);
 }

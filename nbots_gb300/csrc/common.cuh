@@ -23,6 +23,8 @@
     } while (0)
 
 int nbg_cuda_error(cudaError_t e);
+// Records `text` as the thread's last error message and returns `code`.
+int nbg_error_text(int code, const char* text);
 
 namespace nbg {
 
