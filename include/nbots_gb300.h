@@ -218,6 +218,39 @@ int nbg_cg_mixed(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_it
                  double tol, double delta, unsigned flags, nbg_mixed_result_t *result,
                  void *ws, size_t ws_bytes, void *stream);
 
+/* Batched mixed-precision CG: n_sys independent systems stored as one
+ * block-diagonal layout A, system i owning slices [slice_ptr[i],
+ * slice_ptr[i+1]) (its node rows start on a multiple of 32), solved side by
+ * side by one cooperative launch in which each system has its own group of
+ * blocks, barrier, reductions and stopping test.  A launch (x = 0, the
+ * solve, then the optional SIMP compliance sensitivities with a = b = x) is
+ * one CUDA graph replayed on `stream`.  Blocks are shared out in
+ * proportion to slices^gamma (nbg_mixed_batch_plan, gamma 1 at creation);
+ * nbg_mixed_batch_tune times one launch per candidate gamma and keeps the
+ * fastest.  Every system needs a co-resident block: n_sys is at most the
+ * launch's resident block count.  No counterpart in nbots. */
+typedef struct nbg_mixed_batch nbg_mixed_batch_t;
+int nbg_mixed_batch_create(nbg_mixed_batch_t **out, const nbg_bsr_t *A, const double *b,
+                           double *x, uint32_t n_sys, const uint32_t *slice_ptr,
+                           uint32_t max_iter, double tol, double delta, unsigned flags,
+                           void *stream);
+void nbg_mixed_batch_destroy(nbg_mixed_batch_t *m);
+int nbg_mixed_batch_plan(nbg_mixed_batch_t *m, double gamma);
+/* Total blocks of the launch; blocks[i] per system and the gamma in use. */
+uint32_t nbg_mixed_batch_blocks(const nbg_mixed_batch_t *m, uint32_t *blocks, double *gamma);
+int nbg_mixed_batch_set_sensitivity(nbg_mixed_batch_t *m, uint32_t nen, uint32_t N_elem,
+                                    const double *nod, const uint32_t *conn, double nu,
+                                    double thickness, const double *rho, double penal,
+                                    double E0, double Emin, double *dJ);
+/* Asynchronous: one graph launch on the batch's stream. */
+int nbg_mixed_batch_launch(nbg_mixed_batch_t *m);
+/* Waits for the stream; per-system results and b.u (the compliance F^T u
+ * when b is the load vector).  Returns the first error status, else 1 if
+ * some system did not converge, else 0. */
+int nbg_mixed_batch_results(nbg_mixed_batch_t *m, nbg_mixed_result_t *res, double *J);
+int nbg_mixed_batch_tune(nbg_mixed_batch_t *m, uint32_t n_cand, const double *gammas,
+                         double *ms);
+
 /* ------------------------------------------------- host-buffer solver */
 /* A CSR system in host memory (nb_sparse_create layout) solved on the GPU.
  * Device buffers persist in the context between calls; with
@@ -318,6 +351,32 @@ int nbg_fem_solve_mixed(nbg_fem_t *f, uint32_t max_iter, double tol, double delt
 int nbg_fem_strain(nbg_fem_t *f);
 int nbg_fem_stress(nbg_fem_t *f);
 
+/* ------------------------------------------------------------------ SIMP */
+/* SIMP element sensitivities (no counterpart in nbots): with
+ * E_e = Emin + rho_e^p (E0 - Emin), out[e] = -p rho_e^(p-1) (E0 - Emin)
+ * a_e^T Ke0_e b_e, Ke0_e the element stiffness for E = 1 (device arrays). */
+int nbg_simp_sensitivity_f64(uint32_t nen, uint32_t N_elem, const double *nod,
+                             const uint32_t *conn, double nu, double thickness,
+                             const double *rho, double penal, double E0, double Emin,
+                             const double *a, const double *b, double *out, void *stream);
+
+#define NBG_SIMP_COMPLIANCE 0   /* J = F^T u (self-adjoint) */
+#define NBG_SIMP_DOF 1          /* J = u[dof], one adjoint solve K lambda = e_dof */
+
+typedef struct {
+    double J;
+    uint32_t fwd_iters, adj_iters;
+    int status;
+} nbg_simp_info_t;
+
+/* Objective and its gradient for densities rho (host arrays): assemble with
+ * E(rho), apply the boundary conditions (homogeneous Dirichlet values),
+ * solve K u = F (and K lambda = e_dof) with `method` (NBG_METHOD_FP64 or
+ * NBG_METHOD_MIXED) to relative tolerance tol, write dJ/drho to dJ. */
+int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double nu,
+                 double thickness, double penal, double E0, double Emin, int objective,
+                 uint32_t dof, double tol, int method, double *dJ, nbg_simp_info_t *info);
+
 #define NBG_FEM_ROW_PTR 0   /* uint32[N+1] */
 #define NBG_FEM_COL_IDX 1   /* uint32[nnz] */
 #define NBG_FEM_K 2         /* double[nnz] */
@@ -326,11 +385,48 @@ int nbg_fem_stress(nbg_fem_t *f);
 #define NBG_FEM_STRAIN 5    /* double[3 N_gp N_elem] */
 #define NBG_FEM_STRESS 6    /* double[3 N_gp N_elem] */
 #define NBG_FEM_E 7         /* double[N_elem] */
+#define NBG_FEM_NOD 8       /* double[2 N_nod] */
+#define NBG_FEM_CONN 9      /* uint32[nen N_elem] */
 /* Device pointer of one array, and a copy of it to host memory. */
 void *nbg_fem_device_ptr(nbg_fem_t *f, int what);
 size_t nbg_fem_bytes(const nbg_fem_t *f, int what);
 int nbg_fem_download(nbg_fem_t *f, int what, void *host);
 int nbg_fem_upload(nbg_fem_t *f, int what, const void *host);
+
+/* ----------------------------------------------------------------- batch */
+/* Independent FEM problems (meshes of uneven size, each with its own
+ * boundary conditions, densities and loads) merged into one block-diagonal
+ * system and solved side by side by nbg_mixed_batch_* with the SIMP
+ * compliance sensitivities, one CUDA graph per launch.  Instance k's nodes
+ * start at node_off[k], a multiple of 32; the padding nodes before the next
+ * instance are fixed by Dirichlet conditions (identity rows, zero load).
+ * Each instance's K and F equal, bit for bit, those nbg_fem_* builds for it
+ * alone.  The mesh and bc arrays are copied at creation.  All meshes share
+ * one element type.  No counterpart in nbots. */
+typedef struct nbg_batch nbg_batch_t;
+int nbg_batch_create(nbg_batch_t **out, uint32_t n_inst, const nbg_mesh_t *meshes,
+                     const nbg_bcs_t *bcs, void *stream);
+void nbg_batch_destroy(nbg_batch_t *b);
+uint32_t nbg_batch_size(const nbg_batch_t *b);
+/* n_inst + 1 offsets each (node_off in nodes, elem_off in elements);
+ * either may be NULL. */
+int nbg_batch_offsets(const nbg_batch_t *b, uint32_t *node_off, uint32_t *elem_off);
+nbg_fem_t *nbg_batch_fem(nbg_batch_t *b);
+nbg_mixed_batch_t *nbg_batch_solver(nbg_batch_t *b);
+/* E = Emin + rho^p (E0 - Emin) per merged element (host array), assembly,
+ * every instance's boundary conditions (factor 1), block layout. */
+int nbg_batch_assemble_simp(nbg_batch_t *b, const double *rho, double nu, double thickness,
+                            double penal, double E0, double Emin);
+/* (Re)creates the batched solver on the assembled system: mixed CG per
+ * instance, NBG_CG_RELATIVE in flags for ||r|| <= tol ||F_k||. */
+int nbg_batch_setup(nbg_batch_t *b, uint32_t max_iter, double tol, double delta,
+                    unsigned flags);
+/* One graph launch (asynchronous): u = 0, solve, sensitivities. */
+int nbg_batch_launch(nbg_batch_t *b);
+/* Waits; per-instance results and compliance F_k^T u_k. */
+int nbg_batch_results(nbg_batch_t *b, nbg_mixed_result_t *res, double *J);
+/* dJ/drho of each instance's compliance, per merged element (host array). */
+int nbg_batch_sensitivities(nbg_batch_t *b, double *dJ);
 
 #ifdef __cplusplus
 }

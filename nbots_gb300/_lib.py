@@ -43,6 +43,11 @@ class SolveInfo(C.Structure):
                 ("relres", C.c_double), ("tol_reached", C.c_double)]
 
 
+class SimpInfo(C.Structure):
+    _fields_ = [("J", C.c_double), ("fwd_iters", C.c_uint32), ("adj_iters", C.c_uint32),
+                ("status", C.c_int)]
+
+
 class Mesh(C.Structure):
     _fields_ = [("nen", u32), ("N_nod", u32), ("N_elem", u32), ("N_edg", u32),
                 ("nod", vp), ("conn", vp), ("edg", vp)]
@@ -103,6 +108,10 @@ SIGS = {
     "nbg_solver_solve": ([vp, vp, vp, u32, f64, C.c_uint, i32, C.POINTER(SolveInfo)], i32),
     "nbg_host_alloc": ([C.POINTER(vp), sz], i32),
     "nbg_host_free": ([vp], i32),
+    "nbg_simp_sensitivity_f64": ([u32, u32, vp, vp, f64, f64, vp, f64, f64, f64, vp, vp, vp,
+                                  vp], i32),
+    "nbg_fem_simp": ([vp, vp, vp, f64, f64, f64, f64, f64, i32, u32, f64, i32, vp,
+                      C.POINTER(SimpInfo)], i32),
     "nbg_host_pattern": ([vp, vp, vp], i32),
     "nbg_host_incidence": ([vp, vp, vp, vp], i32),
     "nbg_fem_create": ([C.POINTER(vp), vp, vp], i32),
@@ -118,9 +127,31 @@ SIGS = {
     "nbg_fem_bytes": ([vp, i32], sz),
     "nbg_fem_download": ([vp, i32, vp], i32),
     "nbg_fem_upload": ([vp, i32, vp], i32),
+    "nbg_mixed_batch_create": ([C.POINTER(vp), C.POINTER(Bsr), vp, vp, u32, vp, u32, f64, f64,
+                                C.c_uint, vp], i32),
+    "nbg_mixed_batch_destroy": ([vp], None),
+    "nbg_mixed_batch_plan": ([vp, f64], i32),
+    "nbg_mixed_batch_blocks": ([vp, vp, C.POINTER(f64)], u32),
+    "nbg_mixed_batch_set_sensitivity": ([vp, u32, u32, vp, vp, f64, f64, vp, f64, f64, f64, vp],
+                                        i32),
+    "nbg_mixed_batch_launch": ([vp], i32),
+    "nbg_mixed_batch_results": ([vp, vp, vp], i32),
+    "nbg_mixed_batch_tune": ([vp, u32, vp, vp], i32),
+    "nbg_batch_create": ([C.POINTER(vp), u32, vp, vp, vp], i32),
+    "nbg_batch_destroy": ([vp], None),
+    "nbg_batch_size": ([vp], u32),
+    "nbg_batch_offsets": ([vp, vp, vp], i32),
+    "nbg_batch_fem": ([vp], vp),
+    "nbg_batch_solver": ([vp], vp),
+    "nbg_batch_assemble_simp": ([vp, vp, f64, f64, f64, f64, f64], i32),
+    "nbg_batch_setup": ([vp, u32, f64, f64, C.c_uint], i32),
+    "nbg_batch_launch": ([vp], i32),
+    "nbg_batch_results": ([vp, vp, vp], i32),
+    "nbg_batch_sensitivities": ([vp, vp], i32),
 }
 
-FEM_ROW_PTR, FEM_COL_IDX, FEM_K, FEM_F, FEM_U, FEM_STRAIN, FEM_STRESS, FEM_E = range(8)
+(FEM_ROW_PTR, FEM_COL_IDX, FEM_K, FEM_F, FEM_U, FEM_STRAIN, FEM_STRESS, FEM_E, FEM_NOD,
+ FEM_CONN) = range(10)
 CG_JACOBI, CG_RELATIVE = 1, 2
 METHOD_NBOTS, METHOD_FP64, METHOD_MIXED = 0, 1, 2
 PATTERN_SAME = 1

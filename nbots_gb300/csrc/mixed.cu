@@ -25,7 +25,12 @@
 // rebuilding z + beta p for the columns it reads) measured slower, 77 vs
 // 66 us per iteration at 1M dof, because the float-float rebuild per column
 // costs more issue slots and gather bytes than the barrier it saves.
+#include <algorithm>
+#include <cmath>
 #include <cstdint>
+#include <cstring>
+#include <new>
+#include <vector>
 
 #include "persist.cuh"
 
@@ -47,14 +52,17 @@ struct MixArgs {
     __nv_bfloat16* pl;
     float *r, *wh, *xh, *xl;  // own-row vectors when they do not fit in shared memory
     __nv_bfloat16* wl;
-    double* part;  // L1 [0,K), L2 [K,3K), init/update [3K,6K)
+    double* part;  // L1 [0,K), L2 [K,3K), init/update [3K,6K), K = pstride
     unsigned* bar;
     int* status;
-    double* res;  // niter, updates, status, rr64, bb
+    double* res;  // niter, updates, status, rr64, bb, b.u
     uint32_t max_iter;
     double tol, delta;
     unsigned flags;
-    int resident;  // own-row vectors live in shared memory
+    int resident;             // own-row vectors live in shared memory
+    uint32_t s_begin, s_end;  // this system's slices
+    uint32_t g_base, g_size;  // this system's blocks in the launch
+    uint32_t pstride;
 };
 
 __device__ __forceinline__ float bf_round(float x) {
@@ -159,22 +167,24 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
     }
 }
 
-__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed(MixArgs a) {
-    extern __shared__ __align__(16) unsigned char smem[];
+// The solver of one system on the blocks [g_base, g_base + g_size) of the
+// launch: its own slices, group barrier, partial sums and result.
+__device__ __forceinline__ void mixed_solve(const MixArgs& a, unsigned char* smem) {
     __shared__ double red[3 * 32];
     __shared__ double bc[3];
-    const unsigned G = gridDim.x;
+    const unsigned G = a.g_size;
+    const uint32_t rank = blockIdx.x - a.g_base;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nw = kPersistThreads / 32;
     uint32_t s0, s1;
-    slice_range(a.A.n_slices, s0, s1);
+    group_slice_range(a.s_begin, a.s_end, rank, G, s0, s1);
     const uint32_t Nn = a.A.Nn;
     const Own o = own_vectors(a, smem, s0, (s1 - s0) * 32);
     float2* __restrict__ gph = reinterpret_cast<float2*>(a.ph);
     __nv_bfloat162* __restrict__ gpl = reinterpret_cast<__nv_bfloat162*>(a.pl);
     double* const part0 = a.part;
-    double* const part1 = a.part + kMaxBlocks;
-    double* const part2 = a.part + 3 * kMaxBlocks;
+    double* const part1 = a.part + a.pstride;
+    double* const part2 = a.part + 3 * a.pstride;
 
     uint32_t k = 0, nupd = 0;
     double rr64 = 0.0, bb = 0.0, target2 = 0.0, rz = 0.0, rr = 0.0, rmax2 = 0.0;
@@ -194,12 +204,12 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed
         true_residual(a, o, s0, s1, rrl, rzk, &bbl, true);
         const FF t = rzk.result();
         double v[3] = {rrl, bbl, (double)t.hi + (double)t.lo};
-        publish<3>(v, red, part2);
+        group_publish<3>(v, red, part2, rank);
     }
     if (grid_barrier(a.bar, G, a.status)) goto done;
     {
         double t[3];
-        grid_reduce<3>(part2, t, bc);
+        group_reduce<3>(part2, G, t, bc);
         rr64 = t[0];
         bb = t[1];
         rz = t[2];
@@ -227,11 +237,11 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed
                 }
                 const FF t = pw.result();
                 double v[1] = {(double)t.hi + (double)t.lo};
-                publish<1>(v, red, part0);
+                group_publish<1>(v, red, part0, rank);
             }
             if (grid_barrier(a.bar, G, a.status)) goto done;
             double pwd;
-            grid_reduce<1>(part0, &pwd, bc);
+            group_reduce<1>(part0, G, &pwd, bc);
             const FF alpha = ff_from_double(rz / pwd);
             {   // L2: x += alpha p, r -= alpha w, z = r / Aii (own rows only)
                 FFAcc rzk{0.f, 0.f}, rrk{0.f, 0.f};
@@ -259,11 +269,11 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed
                 }
                 const FF t1 = rzk.result(), t2 = rrk.result();
                 double v[2] = {(double)t1.hi + (double)t1.lo, (double)t2.hi + (double)t2.lo};
-                publish<2>(v, red, part1);
+                group_publish<2>(v, red, part1, rank);
             }
             if (grid_barrier(a.bar, G, a.status)) goto done;
             double t2[2];
-            grid_reduce<2>(part1, t2, bc);
+            group_reduce<2>(part1, G, t2, bc);
             double rz_new = t2[0];
             rr = t2[1];
             if (rr > rmax2) rmax2 = rr;
@@ -288,10 +298,10 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed
                 true_residual(a, o, s0, s1, rrl, rzk, nullptr, false);
                 const FF t = rzk.result();
                 double v[2] = {rrl, (double)t.hi + (double)t.lo};
-                publish<2>(v, red, part2);
+                group_publish<2>(v, red, part2, rank);
                 if (grid_barrier(a.bar, G, a.status)) goto done;
                 double tt[2];
-                grid_reduce<2>(part2, tt, bc);
+                group_reduce<2>(part2, G, tt, bc);
                 rr64 = tt[0];
                 rz_new = tt[1];
                 rr = rmax2 = rr64;
@@ -321,8 +331,25 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed
             if (grid_barrier(a.bar, G, a.status)) goto done;
         }
     }
+    {   // b.u in FP64 (the compliance F^T u when b is the load vector).  part0
+        // was last read before the L2 barrier of the last iteration.
+        const double2* __restrict__ u = reinterpret_cast<const double2*>(a.u);
+        const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
+        double bu = 0.0;
+        for (uint32_t s = s0 + warp; s < s1; s += nw) {
+            const uint32_t i = s * 32 + lane;
+            if (i >= Nn) continue;
+            const double2 ui = u[i], bi = b[i];
+            bu = fma(bi.x, ui.x, fma(bi.y, ui.y, bu));
+        }
+        double v[1] = {bu};
+        group_publish<1>(v, red, part0, rank);
+        if (grid_barrier(a.bar, G, a.status)) goto done;
+        group_reduce<1>(part0, G, &bu, bc);
+        if (rank == 0 && threadIdx.x == 0) a.res[5] = bu;
+    }
 done:
-    if (blockIdx.x == 0 && threadIdx.x == 0) {
+    if (rank == 0 && threadIdx.x == 0) {
         a.res[0] = (double)k;
         a.res[1] = (double)nupd;
         int st = ld_volatile(a.status);
@@ -330,6 +357,21 @@ done:
         a.res[3] = rr64;
         a.res[4] = bb;
     }
+}
+
+__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed(MixArgs a) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    mixed_solve(a, smem);
+}
+
+// Many independent systems in one launch: block b solves many[block_of[b]].
+__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
+    k_cg_mixed_many(const MixArgs* __restrict__ many, const uint32_t* __restrict__ block_of) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    __shared__ MixArgs sa;
+    if (threadIdx.x == 0) sa = many[block_of[blockIdx.x]];
+    __syncthreads();
+    mixed_solve(sa, smem);
 }
 
 size_t mixed_bytes(uint32_t N) {
@@ -389,6 +431,11 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
         rc = coop_grid_resident((const void*)k_cg_mixed, A->n_slices,
                                 NBG_MIXED_RESIDENT ? 56 * 32 : 0, &G, &dyn);
     a.resident = dyn > 0;
+    a.s_begin = 0;
+    a.s_end = A->n_slices;
+    a.g_base = 0;
+    a.g_size = G;
+    a.pstride = kMaxBlocks;
     if (e == cudaSuccess && rc == NBG_OK) {
         void* args[] = {&a};
         e = cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(G), dim3(kPersistThreads),
@@ -408,4 +455,403 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     }
     if (own) cudaFree(own);
     return rc;
+}
+
+// ------------------------------------------------------------------ batch
+// Many independent systems stored as one block-diagonal layout (each
+// system's node rows start on a slice boundary) and solved by one
+// cooperative launch of k_cg_mixed_many, replayed as a CUDA graph together
+// with zeroing x and, optionally, the SIMP compliance sensitivities.
+
+struct nbg_mixed_batch {
+    nbg_bsr_t A;
+    const double* b;
+    double* x;
+    uint32_t n_sys;
+    std::vector<uint32_t> slice_ptr, blocks;
+    uint32_t max_iter;
+    double tol, delta, gamma;
+    unsigned flags;
+    cudaStream_t stream;
+    void* ws;
+    MixArgs* d_args;
+    uint32_t* d_map;
+    double* d_res;
+    unsigned char* d_state;
+    unsigned G;
+    size_t dyn;
+    // compliance sensitivities after the solve (a = b = x)
+    bool sens;
+    uint32_t nen, N_elem;
+    const double* nod;
+    const uint32_t* conn;
+    const double* rho;
+    double* dJ;
+    double nu, thickness, penal, E0, Emin;
+    cudaGraph_t graph;
+    cudaGraphExec_t exec;
+};
+
+namespace {
+
+constexpr size_t kStateStride = 256;  // per system: barrier at +0, status at +128
+constexpr size_t kResStride = 8;      // doubles of result per system
+
+size_t batch_bytes(uint32_t N, uint32_t n_sys) {
+    return mixed_bytes(N) + align256((size_t)n_sys * kStateStride) +
+           align256((size_t)n_sys * kResStride * 8) + align256((size_t)n_sys * sizeof(MixArgs)) +
+           align256((size_t)kMaxBlocks * 4);
+}
+
+// Vector slots of the workspace shared by every system (indexed by the
+// global node row).
+void bind_vectors(MixArgs& a, char* base, uint32_t N) {
+    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 2);
+    a.r = (float*)base;
+    a.ph = (float*)(base + f);
+    a.wh = (float*)(base + 2 * f);
+    a.xh = (float*)(base + 3 * f);
+    a.xl = (float*)(base + 4 * f);
+    a.pl = (__nv_bfloat16*)(base + 5 * f);
+    a.wl = (__nv_bfloat16*)(base + 5 * f + h);
+    a.part = (double*)(base + 5 * f + 2 * h);
+}
+
+// Blocks per system: one each, then one at a time to the system with the
+// largest weight per block (weight = slices^gamma), never more blocks than
+// warps of slices.  Minimises the largest weight per block.
+void share_blocks(const std::vector<uint32_t>& sp, double gamma, unsigned total,
+                  std::vector<uint32_t>& out) {
+    const size_t n = sp.size() - 1;
+    const uint32_t nw = kPersistThreads / 32;
+    std::vector<double> w(n);
+    std::vector<uint32_t> cap(n);
+    out.assign(n, 1);
+    for (size_t i = 0; i < n; i++) {
+        const uint32_t S = sp[i + 1] - sp[i];
+        w[i] = std::pow((double)std::max<uint32_t>(S, 1), gamma);
+        cap[i] = std::max<uint32_t>(1, (S + nw - 1) / nw);
+    }
+    for (unsigned left = total - (unsigned)n; left > 0; --left) {
+        size_t best = n;
+        double bw = -1.0;
+        for (size_t i = 0; i < n; i++)
+            if (out[i] < cap[i] && w[i] / out[i] > bw) {
+                bw = w[i] / out[i];
+                best = i;
+            }
+        if (best == n) break;
+        out[best]++;
+    }
+}
+
+uint32_t max_slices_per_block(const std::vector<uint32_t>& sp, const std::vector<uint32_t>& bl) {
+    uint32_t m = 0;
+    for (size_t i = 0; i + 1 < sp.size(); i++)
+        m = std::max(m, (sp[i + 1] - sp[i] + bl[i] - 1) / bl[i]);
+    return m;
+}
+
+inline int cu(cudaError_t e) { return e == cudaSuccess ? NBG_OK : nbg_cuda_error(e); }
+
+void drop_graph(nbg_mixed_batch* m) {
+    if (m->exec) cudaGraphExecDestroy(m->exec);
+    if (m->graph) cudaGraphDestroy(m->graph);
+    m->exec = nullptr;
+    m->graph = nullptr;
+}
+
+// Block shares, launch size and the per-system argument table for `gamma`.
+int batch_plan(nbg_mixed_batch* m, double gamma) {
+    const void* fn = (const void*)k_cg_mixed_many;
+    int dev = 0, nsm = 0, optin = 0;
+    NBG_CHECK(cudaGetDevice(&dev));
+    NBG_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+    NBG_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
+    cudaFuncAttributes fa;
+    NBG_CHECK(cudaFuncGetAttributes(&fa, fn));
+    const uint32_t n = m->n_sys;
+    std::vector<uint32_t> bl;
+    unsigned G = 0;
+    size_t dyn = 0;
+    // own rows in shared memory when every block's rows fit
+    for (int per_sm = kPersistMinBlocks; NBG_MIXED_RESIDENT && per_sm >= 1 && !G; --per_sm) {
+        const unsigned total = std::min<unsigned>((unsigned)nsm * per_sm, kMaxBlocks);
+        if (n > total) break;
+        share_blocks(m->slice_ptr, gamma, total, bl);
+        const size_t bytes = (size_t)max_slices_per_block(m->slice_ptr, bl) * 56 * 32;
+        if (bytes + fa.sharedSizeBytes > (size_t)optin) continue;
+        NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
+        int occ = 0;
+        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, bytes));
+        unsigned used = 0;
+        for (uint32_t v : bl) used += v;
+        if ((unsigned)occ * (unsigned)nsm >= used) {
+            G = used;
+            dyn = bytes;
+        }
+    }
+    if (!G) {
+        NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 0));
+        int occ = 0;
+        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, 0));
+        const unsigned total = std::min<unsigned>((unsigned)nsm * (unsigned)std::max(occ, 1), kMaxBlocks);
+        if (n > total) return NBG_ERR_ARG;  // every system needs a co-resident block
+        share_blocks(m->slice_ptr, gamma, total, bl);
+        for (uint32_t v : bl) G += v;
+        dyn = 0;
+    }
+    // argument table and block -> system map
+    std::vector<MixArgs> args(n);
+    std::vector<uint32_t> map(G);
+    char* base = (char*)m->ws;
+    unsigned g = 0;
+    for (uint32_t i = 0; i < n; i++) {
+        MixArgs& a = args[i];
+        memset(&a, 0, sizeof(a));
+        a.A = m->A;
+        a.b = m->b;
+        a.u = m->x;
+        bind_vectors(a, base, m->A.N);
+        a.part += 6 * (size_t)g;
+        a.pstride = bl[i];
+        a.bar = (unsigned*)(m->d_state + i * kStateStride);
+        a.status = (int*)(m->d_state + i * kStateStride + 128);
+        a.res = m->d_res + i * kResStride;
+        a.max_iter = m->max_iter;
+        a.tol = m->tol;
+        a.delta = m->delta;
+        a.flags = m->flags;
+        a.resident = dyn > 0;
+        a.s_begin = m->slice_ptr[i];
+        a.s_end = m->slice_ptr[i + 1];
+        a.g_base = g;
+        a.g_size = bl[i];
+        for (uint32_t k = 0; k < bl[i]; k++) map[g + k] = i;
+        g += bl[i];
+    }
+    NBG_CHECK(cudaMemcpy(m->d_args, args.data(), n * sizeof(MixArgs), cudaMemcpyHostToDevice));
+    NBG_CHECK(cudaMemcpy(m->d_map, map.data(), G * 4, cudaMemcpyHostToDevice));
+    m->blocks = bl;
+    m->G = G;
+    m->dyn = dyn;
+    m->gamma = gamma;
+    drop_graph(m);
+    return NBG_OK;
+}
+
+// The work of one batch launch, enqueued on s (captured into the graph).
+cudaError_t batch_enqueue(nbg_mixed_batch* m, cudaStream_t s) {
+    cudaError_t e = cudaMemsetAsync(m->x, 0, 8 * (size_t)m->A.N, s);
+    if (e == cudaSuccess) e = cudaMemsetAsync(m->d_state, 0, (size_t)m->n_sys * kStateStride, s);
+    if (e != cudaSuccess) return e;
+    cudaLaunchConfig_t cfg = {};
+    cfg.gridDim = dim3(m->G);
+    cfg.blockDim = dim3(kPersistThreads);
+    cfg.dynamicSmemBytes = m->dyn;
+    cfg.stream = s;
+    cudaLaunchAttribute attr[1];
+    attr[0].id = cudaLaunchAttributeCooperative;
+    attr[0].val.cooperative = 1;
+    cfg.attrs = attr;
+    cfg.numAttrs = 1;
+    const MixArgs* args = m->d_args;
+    const uint32_t* map = m->d_map;
+    e = cudaLaunchKernelEx(&cfg, k_cg_mixed_many, args, map);
+    if (e != cudaSuccess || !m->sens) return e;
+    const int rc = nbg_simp_sensitivity_f64(m->nen, m->N_elem, m->nod, m->conn, m->nu,
+                                            m->thickness, m->rho, m->penal, m->E0, m->Emin, m->x,
+                                            m->x, m->dJ, s);
+    return rc == NBG_OK ? cudaSuccess : cudaErrorLaunchFailure;
+}
+
+// The function attribute is shared by every batch in the process: set it
+// to this batch's size before capturing and before each replay.
+int set_smem(const nbg_mixed_batch* m) {
+    NBG_CHECK(cudaFuncSetAttribute((const void*)k_cg_mixed_many,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->dyn));
+    return NBG_OK;
+}
+
+int build_graph(nbg_mixed_batch* m) {
+    const int rc = set_smem(m);
+    if (rc != NBG_OK) return rc;
+    cudaStream_t cap;
+    NBG_CHECK(cudaStreamCreateWithFlags(&cap, cudaStreamNonBlocking));
+    cudaError_t e = cudaStreamBeginCapture(cap, cudaStreamCaptureModeThreadLocal);
+    if (e == cudaSuccess) {
+        const cudaError_t e1 = batch_enqueue(m, cap);
+        cudaGraph_t g = nullptr;
+        const cudaError_t e2 = cudaStreamEndCapture(cap, &g);
+        e = e1 != cudaSuccess ? e1 : e2;
+        if (e == cudaSuccess) {
+            m->graph = g;
+            e = cudaGraphInstantiate(&m->exec, g, 0);
+        } else if (g) {
+            cudaGraphDestroy(g);
+        }
+    }
+    cudaStreamDestroy(cap);
+    if (e != cudaSuccess) {
+        drop_graph(m);
+        return nbg_cuda_error(e);
+    }
+    return NBG_OK;
+}
+
+}  // namespace
+
+extern "C" int nbg_mixed_batch_create(nbg_mixed_batch_t** out, const nbg_bsr_t* A,
+                                      const double* b, double* x, uint32_t n_sys,
+                                      const uint32_t* slice_ptr, uint32_t max_iter, double tol,
+                                      double delta, unsigned flags, void* stream) {
+    if (!out) return NBG_ERR_ARG;
+    *out = nullptr;
+    if (!A || !b || !x || !slice_ptr || n_sys == 0 || n_sys > kMaxBlocks || !A->b64 ||
+        !A->b32 || !A->blo || !A->dinv32 || !(delta > 0.0 && delta < 1.0))
+        return NBG_ERR_ARG;
+    if (slice_ptr[0] != 0 || slice_ptr[n_sys] != A->n_slices) return NBG_ERR_ARG;
+    for (uint32_t i = 0; i < n_sys; i++)
+        if (slice_ptr[i + 1] < slice_ptr[i]) return NBG_ERR_ARG;
+    nbg_mixed_batch* m = new (std::nothrow) nbg_mixed_batch();
+    if (!m) return NBG_ERR_NOMEM;
+    m->A = *A;
+    m->b = b;
+    m->x = x;
+    m->n_sys = n_sys;
+    m->slice_ptr.assign(slice_ptr, slice_ptr + n_sys + 1);
+    m->max_iter = max_iter;
+    m->tol = tol;
+    m->delta = delta;
+    m->flags = flags;
+    m->stream = (cudaStream_t)stream;
+    const size_t need = batch_bytes(A->N, n_sys);
+    cudaError_t e = cudaMalloc(&m->ws, need);
+    if (e != cudaSuccess) {
+        delete m;
+        return nbg_cuda_error(e);
+    }
+    char* p = (char*)m->ws + mixed_bytes(A->N);
+    m->d_state = (unsigned char*)p;
+    p += align256((size_t)n_sys * kStateStride);
+    m->d_res = (double*)p;
+    p += align256((size_t)n_sys * kResStride * 8);
+    m->d_args = (MixArgs*)p;
+    p += align256((size_t)n_sys * sizeof(MixArgs));
+    m->d_map = (uint32_t*)p;
+    int rc = batch_plan(m, 1.0);
+    if (rc != NBG_OK) {
+        nbg_mixed_batch_destroy(m);
+        return rc;
+    }
+    *out = m;
+    return NBG_OK;
+}
+
+extern "C" void nbg_mixed_batch_destroy(nbg_mixed_batch_t* m) {
+    if (!m) return;
+    drop_graph(m);
+    if (m->ws) cudaFree(m->ws);
+    delete m;
+}
+
+extern "C" int nbg_mixed_batch_plan(nbg_mixed_batch_t* m, double gamma) {
+    if (!m || !(gamma >= 0.0 && gamma <= 4.0)) return NBG_ERR_ARG;
+    return batch_plan(m, gamma);
+}
+
+extern "C" uint32_t nbg_mixed_batch_blocks(const nbg_mixed_batch_t* m, uint32_t* blocks,
+                                           double* gamma) {
+    if (!m) return 0;
+    if (blocks) std::copy(m->blocks.begin(), m->blocks.end(), blocks);
+    if (gamma) *gamma = m->gamma;
+    return m->G;
+}
+
+extern "C" int nbg_mixed_batch_set_sensitivity(nbg_mixed_batch_t* m, uint32_t nen,
+                                               uint32_t N_elem, const double* nod,
+                                               const uint32_t* conn, double nu, double thickness,
+                                               const double* rho, double penal, double E0,
+                                               double Emin, double* dJ) {
+    if (!m || (nen != 3 && nen != 4) || (N_elem && (!nod || !conn || !rho || !dJ)))
+        return NBG_ERR_ARG;
+    m->sens = N_elem > 0;
+    m->nen = nen;
+    m->N_elem = N_elem;
+    m->nod = nod;
+    m->conn = conn;
+    m->nu = nu;
+    m->thickness = thickness;
+    m->rho = rho;
+    m->penal = penal;
+    m->E0 = E0;
+    m->Emin = Emin;
+    m->dJ = dJ;
+    drop_graph(m);
+    return NBG_OK;
+}
+
+extern "C" int nbg_mixed_batch_launch(nbg_mixed_batch_t* m) {
+    if (!m) return NBG_ERR_ARG;
+    const int rc = m->exec ? set_smem(m) : build_graph(m);
+    if (rc != NBG_OK) return rc;
+    NBG_CHECK(cudaGraphLaunch(m->exec, m->stream));
+    return NBG_OK;
+}
+
+extern "C" int nbg_mixed_batch_results(nbg_mixed_batch_t* m, nbg_mixed_result_t* res,
+                                       double* J) {
+    if (!m) return NBG_ERR_ARG;
+    std::vector<double> h((size_t)m->n_sys * kResStride);
+    NBG_CHECK(cudaMemcpyAsync(h.data(), m->d_res, h.size() * 8, cudaMemcpyDeviceToHost,
+                              m->stream));
+    NBG_CHECK(cudaStreamSynchronize(m->stream));
+    int worst = NBG_OK;
+    for (uint32_t i = 0; i < m->n_sys; i++) {
+        const double* r = &h[(size_t)i * kResStride];
+        nbg_mixed_result_t t;
+        t.niter = (uint32_t)r[0];
+        t.n_updates = (uint32_t)r[1];
+        t.status = (int)r[2];
+        t.bnorm = std::sqrt(r[4]);
+        t.relres = r[4] > 0 ? std::sqrt(r[3] / r[4]) : std::sqrt(r[3]);
+        if (res) res[i] = t;
+        if (J) J[i] = r[5];
+        if (t.status < 0 && worst >= 0) worst = t.status;
+        else if (t.status > 0 && worst == NBG_OK) worst = t.status;
+    }
+    return worst;
+}
+
+extern "C" int nbg_mixed_batch_tune(nbg_mixed_batch_t* m, uint32_t n_cand, const double* gammas,
+                                    double* ms) {
+    if (!m || !n_cand || !gammas) return NBG_ERR_ARG;
+    cudaEvent_t t0, t1;
+    NBG_CHECK(cudaEventCreate(&t0));
+    NBG_CHECK(cudaEventCreate(&t1));
+    int rc = NBG_OK;
+    double best_ms = 0.0, best_g = gammas[0];
+    for (uint32_t c = 0; c < n_cand && rc == NBG_OK; c++) {
+        rc = nbg_mixed_batch_plan(m, gammas[c]);
+        if (rc == NBG_OK) rc = nbg_mixed_batch_launch(m);  // builds the graph, warms up
+        if (rc == NBG_OK) rc = cu(cudaEventRecord(t0, m->stream));
+        if (rc == NBG_OK) rc = nbg_mixed_batch_launch(m);
+        if (rc == NBG_OK) rc = cu(cudaEventRecord(t1, m->stream));
+        if (rc == NBG_OK) rc = cu(cudaEventSynchronize(t1));
+        float t = 0.f;
+        if (rc == NBG_OK) rc = cu(cudaEventElapsedTime(&t, t0, t1));
+        if (rc == NBG_OK) {
+            const int st = nbg_mixed_batch_results(m, nullptr, nullptr);
+            if (st < 0) rc = st;
+        }
+        if (ms) ms[c] = t;
+        if (rc == NBG_OK && (c == 0 || t < best_ms)) {
+            best_ms = t;
+            best_g = gammas[c];
+        }
+    }
+    cudaEventDestroy(t0);
+    cudaEventDestroy(t1);
+    if (rc != NBG_OK) return rc;
+    return nbg_mixed_batch_plan(m, best_g);
 }

@@ -83,6 +83,44 @@ __device__ __forceinline__ void publish(double (&v)[NV], double* red, double* pa
         for (int k = 0; k < NV; k++) part[blockIdx.x * NV + k] = v[k];
 }
 
+// Group flavours, for launches that run independent problems side by side:
+// a group is G consecutive blocks; `rank` is the block's place in it.
+__device__ __forceinline__ void group_slice_range(uint32_t sb, uint32_t se, uint32_t rank,
+                                                  uint32_t G, uint32_t& s0, uint32_t& s1) {
+    const uint64_t S = se - sb;
+    s0 = sb + (uint32_t)((S * rank) / G);
+    s1 = sb + (uint32_t)((S * (rank + 1)) / G);
+}
+
+template <int NV>
+__device__ __forceinline__ void group_publish(double (&v)[NV], double* red, double* part,
+                                              uint32_t rank) {
+    block_sum_plain<NV>(v, red);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[rank * NV + k] = v[k];
+}
+
+template <int NV>
+__device__ __forceinline__ void group_reduce(const double* part, uint32_t G, double* out,
+                                             double* sh) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (unsigned b = lane; b < G; b += 32) s += part[b * NV + k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            if (lane == 0) sh[k] = s;
+        }
+    }
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) out[k] = sh[k];
+    __syncthreads();
+}
+
 // (A x) for node row (s, lane) with FP64 values and FMAs.
 __device__ __forceinline__ double2 spmv_row_f64(const nbg_bsr_t& A, uint32_t s, uint32_t lane,
                                                 const double2* __restrict__ xv) {

@@ -650,6 +650,8 @@ void *nbg_fem_device_ptr(nbg_fem_t *f, int what)
 	case NBG_FEM_STRAIN: return f->strain;
 	case NBG_FEM_STRESS: return f->stress;
 	case NBG_FEM_E: return f->E;
+	case NBG_FEM_NOD: return f->nod;
+	case NBG_FEM_CONN: return f->conn;
 	default: return NULL;
 	}
 }
@@ -665,6 +667,8 @@ size_t nbg_fem_bytes(const nbg_fem_t *f, int what)
 	case NBG_FEM_STRAIN:
 	case NBG_FEM_STRESS: return 8 * 3 * (size_t)n_gp(f) * f->m.N_elem;
 	case NBG_FEM_E: return 8 * (size_t)f->m.N_elem;
+	case NBG_FEM_NOD: return 16 * (size_t)f->m.N_nod;
+	case NBG_FEM_CONN: return 4 * (size_t)f->m.nen * f->m.N_elem;
 	default: return 0;
 	}
 }
@@ -685,4 +689,91 @@ int nbg_fem_upload(nbg_fem_t *f, int what, const void *host)
 		return NBG_ERR_ARG;
 	int rc = nbg_h2d(d, host, nbg_fem_bytes(f, what), f->stream);
 	return rc == NBG_OK ? nbg_stream_sync(f->stream) : rc;
+}
+
+/* ------------------------------------------------------------------ SIMP */
+static int solve_rhs(nbg_fem_t *f, const double *b, double *x, double tol, int method,
+		     uint32_t *iters)
+{
+	int rc = nbg_fem_block_layout(f, NULL);
+	if (rc != NBG_OK)
+		return rc;
+	const size_t need = method == NBG_METHOD_MIXED ? nbg_cg_mixed_workspace_bytes(f->N)
+						      : nbg_cg_bsr_workspace_bytes(f->N);
+	if ((rc = ensure_ws(f, need)) != NBG_OK)
+		return rc;
+	if (method == NBG_METHOD_MIXED) {
+		nbg_mixed_result_t r;
+		rc = nbg_cg_mixed(&f->bsr, b, x, 8 * f->N, tol, 0.1, NBG_CG_JACOBI | NBG_CG_RELATIVE,
+				  &r, f->cg_ws, f->cg_ws_bytes, f->stream);
+		*iters = r.niter;
+	} else {
+		nbg_cg_result_t r;
+		rc = nbg_cg_bsr_f64(&f->bsr, b, x, 8 * f->N, tol, NBG_CG_JACOBI | NBG_CG_RELATIVE,
+				    &r, f->cg_ws, f->cg_ws_bytes, f->stream);
+		*iters = r.niter;
+	}
+	return rc;
+}
+
+int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double nu,
+		 double thickness, double penal, double E0, double Emin, int objective,
+		 uint32_t dof, double tol, int method, double *dJ, nbg_simp_info_t *info)
+{
+	int rc = NBG_OK;
+	const uint32_t Ne = f->m.N_elem, N = f->N;
+	double *E = malloc(8 * (size_t)(Ne ? Ne : 1));
+	double *hu = malloc(8 * (size_t)N), *hF = malloc(8 * (size_t)N);
+	void *d_rho = NULL, *d_lam = NULL, *d_e = NULL, *d_out = NULL;
+	memset(info, 0, sizeof(*info));
+	if (!E || !hu || !hF)
+		TRY(NBG_ERR_NOMEM);
+	if (objective == NBG_SIMP_DOF && dof >= N)
+		TRY(NBG_ERR_ARG);
+	for (uint32_t e = 0; e < Ne; e++)
+		E[e] = Emin + pow(rho[e], penal) * (E0 - Emin);
+	double g0[2] = {0.0, 0.0};
+	TRY(nbg_fem_assemble(f, E, nu, thickness, 0.0, 0, g0, NULL));
+	TRY(nbg_fem_apply_bcs(f, bcs, 1.0));
+	TRY(zero_u(f));
+	TRY(solve_rhs(f, f->F, f->u, tol, method, &info->fwd_iters));
+	TRY(nbg_d2h(hu, f->u, 8 * (size_t)N, f->stream));
+	TRY(nbg_d2h(hF, f->F, 8 * (size_t)N, f->stream));
+	TRY(nbg_stream_sync(f->stream));
+	TRY(nbg_dev_alloc(&d_rho, 8 * (size_t)(Ne ? Ne : 1)));
+	TRY(nbg_dev_alloc(&d_out, 8 * (size_t)(Ne ? Ne : 1)));
+	TRY(nbg_h2d(d_rho, rho, 8 * (size_t)Ne, f->stream));
+	const double *adj = f->u;
+	if (objective == NBG_SIMP_COMPLIANCE) {
+		double J = 0.0;
+		for (uint32_t i = 0; i < N; i++)
+			J += hF[i] * hu[i];
+		info->J = J;
+	} else {
+		info->J = hu[dof];
+		/* adjoint: K lambda = e_dof (K is symmetric after nbots' elimination) */
+		memset(hF, 0, 8 * (size_t)N);
+		hF[dof] = 1.0;
+		memset(hu, 0, 8 * (size_t)N);
+		TRY(nbg_dev_alloc(&d_e, 8 * (size_t)N));
+		TRY(nbg_dev_alloc(&d_lam, 8 * (size_t)N));
+		TRY(nbg_h2d(d_e, hF, 8 * (size_t)N, f->stream));
+		TRY(nbg_h2d(d_lam, hu, 8 * (size_t)N, f->stream));
+		TRY(solve_rhs(f, d_e, d_lam, tol, method, &info->adj_iters));
+		adj = d_lam;
+	}
+	TRY(nbg_simp_sensitivity_f64(f->m.nen, Ne, f->nod, f->conn, nu, thickness, d_rho, penal,
+				     E0, Emin, adj, f->u, d_out, f->stream));
+	TRY(nbg_d2h(dJ, d_out, 8 * (size_t)Ne, f->stream));
+	TRY(nbg_stream_sync(f->stream));
+fail:
+	info->status = rc;
+	free(E);
+	free(hu);
+	free(hF);
+	nbg_dev_free(d_rho);
+	nbg_dev_free(d_lam);
+	nbg_dev_free(d_e);
+	nbg_dev_free(d_out);
+	return rc;
 }
