@@ -147,6 +147,127 @@ def run_reference(args):
 
 
 # ------------------------------------------------------------------ GPU
+def bench_c4(lib, L, W):
+    """SIMP gradients on the 512x256 grid (rho ~ U(0.3,0.7), p = 3): wall time
+    of one objective + gradient through nbg_fem_simp (assembly, boundary
+    conditions, forward solve, adjoint solve for the one-dof objective,
+    sensitivity kernel, copies), mixed precision and FP64 at relres 1e-8,
+    and the mixed gradients' deviation from FP64 ones at relres 1e-12."""
+    from nbots_gb300.simp import COMPLIANCE, DOF, SimpProblem
+    p = W.config_c4()
+    rho = p.meta["rho"]
+    nx, ny = p.meta["nx"], p.meta["ny"]
+    dof = 2 * ((ny // 2) * (nx + 1) + nx)  # x-displacement of the right-edge midpoint
+    out = {"workload": f"C4: {nx}x{ny} Q4 SIMP, {p.n_dof} dof, rho~U(0.3,0.7) seed 4, p=3, "
+                       "Emin=1e-9, E0=1; objectives compliance and u_x of the right-edge "
+                       "midpoint"}
+    ref = SimpProblem(p, tol=1e-12, method=L.METHOD_FP64)
+    for name, obj in (("compliance", COMPLIANCE), ("u_x_output", DOF)):
+        _, g64, _ = ref.evaluate(rho, obj, dof)
+        row = {}
+        for mname, m in (("mixed", L.METHOD_MIXED), ("fp64", L.METHOD_FP64)):
+            sp_ = SimpProblem(p, tol=1e-8, method=m)
+            sp_.evaluate(rho, obj, dof)  # warm
+            ts = []
+            for _ in range(3):
+                t0 = time.perf_counter()
+                J, g, info = sp_.evaluate(rho, obj, dof)
+                ts.append(time.perf_counter() - t0)
+            row[mname] = {"s_per_gradient": float(np.median(ts)), "fwd_iters": info.fwd_iters,
+                          "adj_iters": info.adj_iters,
+                          "grad_dev_vs_fp64_1e-12": float(np.max(np.abs(g - g64)) /
+                                                          np.max(np.abs(g64)))}
+            sp_.close()
+        out[name] = row
+    ref.close()
+    return out
+
+
+def bench_c5(args, lib, L, W, sp, dev, stream, flush):
+    """96 batched SIMP cantilevers: one graph launch = zero u, batched mixed
+    CG to relres 1e-8 per instance, compliance sensitivities.  Per-instance
+    errors against an FP64 solve of the same merged system to relres 1e-13."""
+    import torch
+    from nbots_gb300.batch import Batch
+    t0 = time.perf_counter()
+    probs = W.config_c5()
+    b = Batch(probs, stream=sp)
+    rho = [p.meta["rho"] for p in probs]
+    b.assemble_simp(rho, nu=probs[0].nu, thickness=probs[0].thickness)
+    b.setup(max_iter=100000, tol=TOL)
+    t_setup = time.perf_counter() - t0
+    gammas = (1.0, 1.25, 1.5, 1.75, 2.0)
+    ms = b.tune(gammas)
+    G, blocks, gamma = b.blocks()
+    for _ in range(args.warmup):
+        b.launch()
+    ts = []
+    for _ in range(args.steps):
+        flush.fill_(4.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        b.launch()
+        e1.record(stream)
+        e1.synchronize()
+        ts.append(e0.elapsed_time(e1) / 1e3)
+    res, J = b.results()
+    us = b.displacements()
+    dJ = b.sensitivities()
+    t = float(np.median(ts))
+    # FP64 reference on the merged system
+    A = L.Bsr()
+    L.check(lib.nbg_fem_block_layout(b.fem, C.byref(A)), "block_layout")
+    N = b.n_dof
+    u64 = torch.zeros(N, dtype=torch.float64, device=dev)
+    wsb = lib.nbg_cg_bsr_workspace_bytes(N)
+    ws = torch.empty(wsb, dtype=torch.uint8, device=dev)
+    r64 = L.CgResult()
+    Fd = lib.nbg_fem_device_ptr(b.fem, L.FEM_F)
+    rc = lib.nbg_cg_bsr_f64(C.byref(A), Fd, u64.data_ptr(), 200000, 1e-13,
+                            L.CG_JACOBI | L.CG_RELATIVE, C.byref(r64), ws.data_ptr(), wsb, sp)
+    assert rc == 0, rc
+    rho_d = torch.from_numpy(np.concatenate(rho)).to(dev)
+    g64 = torch.empty(b.n_elems, dtype=torch.float64, device=dev)
+    L.check(lib.nbg_simp_sensitivity_f64(4, b.n_elems, lib.nbg_fem_device_ptr(b.fem, L.FEM_NOD),
+                                         lib.nbg_fem_device_ptr(b.fem, L.FEM_CONN),
+                                         probs[0].nu, probs[0].thickness, rho_d.data_ptr(), 3.0,
+                                         1.0, 1e-9, u64.data_ptr(), u64.data_ptr(),
+                                         g64.data_ptr(), sp), "sensitivity")
+    torch.cuda.synchronize()
+    u64h, g64h = u64.cpu().numpy(), g64.cpu().numpy()
+    Fh = b.merged(L.FEM_F)
+    eu, eJ, eg = [], [], []
+    for k, p in enumerate(probs):
+        n0 = 2 * int(b.node_off[k])
+        uk = u64h[n0:n0 + p.n_dof]
+        eu.append(float(np.linalg.norm(us[k] - uk) / np.linalg.norm(uk)))
+        Jk = float(Fh[n0:n0 + p.n_dof] @ uk)
+        eJ.append(abs(J[k] - Jk) / abs(Jk))
+        gk = g64h[int(b.elem_off[k]):int(b.elem_off[k + 1])]
+        eg.append(float(np.max(np.abs(dJ[k] - gk)) / np.max(np.abs(gk))))
+    iters = [r.niter for r in res]
+    out = {"workload": "C5: 96 Q4 SIMP cantilevers, sizes U{64x32,128x64,256x128,512x256} "
+                       "seed 5, rho~U(0.2,1.0), 1-4 point loads; mixed CG to relres 1e-8 per "
+                       "instance + compliance gradients, one CUDA graph launch",
+           "instances": len(probs), "dof_total": int(sum(p.n_dof for p in probs)),
+           "dof_merged_padded": N, "s_per_batch": t, "solves_per_s": len(probs) / t,
+           "dof_iters_per_s": float(sum(p.n_dof * r.niter for p, r in zip(probs, res))) / t,
+           "status_all_zero": all(r.status == 0 for r in res),
+           "iters_min_max": [min(iters), max(iters)],
+           "max_relres": max(r.relres for r in res),
+           "err_u_vs_fp64_rel_l2_max": max(eu), "err_u_vs_fp64_rel_l2_median":
+               float(np.median(eu)),
+           "err_compliance_vs_fp64_max": max(eJ), "err_grad_vs_fp64_max": max(eg),
+           "fp64_reference_iters": r64.niter,
+           "autotune": {"gammas": list(gammas), "ms": [float(x) for x in ms], "chosen": gamma,
+                        "blocks": G, "blocks_min_max": [int(blocks.min()), int(blocks.max())]},
+           "setup_s": t_setup, "gpu_launches_per_batch": 2,
+           "l2": "flushed (512 MB write) before every timed launch"}
+    b.close()
+    return out
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -348,6 +469,9 @@ def run_gpu(args):
         dist.all_reduce(vals, op=dist.ReduceOp.MAX)
     t_all, e2e_all = float(vals[0]), float(vals[1])
 
+    c4 = None if args.no_c4 else bench_c4(lib, L, W)
+    c5 = None if args.no_c5 else bench_c5(args, lib, L, W, sp, dev, stream, flush)
+
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
         cpu = cpu_baseline(p)
@@ -379,6 +503,8 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(8 * N),
                     "path": "nbg_solver_set_matrix (values, pattern kept) + nbg_solver_solve "
                             "(mixed) from pinned host buffers"},
+            "c4_simp": c4,
+            "c5_batch": c5,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "clocks": clk.summary(),
@@ -453,6 +579,8 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-c4", action="store_true", help="skip the SIMP gradient timings")
+    ap.add_argument("--no-c5", action="store_true", help="skip the batched solves")
     ap.add_argument("--profile", choices=["mixed", "fp64", "spmv"],
                     help="one bounded kernel launch for ncu instead of the benchmark")
     ap.add_argument("--iters", type=int, default=100)

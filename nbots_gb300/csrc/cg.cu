@@ -115,7 +115,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
     }
     uint32_t k = 0;
     double dot_gg = 0.0, bb = 0.0;
-    if (grid_barrier(a.bar, G, a.status)) goto done;
+    if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
     {
         double t[2];
         grid_reduce<2>(a.partC, t, bc);
@@ -158,7 +158,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
                 a.partA[blockIdx.x * 3 + 1] = v3[1];
                 a.partA[blockIdx.x * 3 + 2] = v3[2];
             }
-            if (grid_barrier(a.bar, G, a.status)) goto done;
+            if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
             double t3[3];
             grid_reduce<3>(a.partA, t3, bc);
             const double dot_pw = t3[0], dot_gq = t3[2];
@@ -176,7 +176,7 @@ __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
             }
             block_sum<1>(v1, red);
             if (threadIdx.x == 0) a.partB[blockIdx.x] = v1[0];
-            if (grid_barrier(a.bar, G, a.status)) goto done;
+            if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
             double t1[1];
             grid_reduce<1>(a.partB, t1, bc);
             beta = dvd(t1[0], dot_gq);

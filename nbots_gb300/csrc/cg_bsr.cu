@@ -5,8 +5,10 @@
 // GB300 issues FP64 at a small fraction of its FP32 rate, so this kernel
 // keeps the FP64 instruction count at one FMA per stored value plus seven
 // per dof (q = g / Aii becomes a multiply by the stored reciprocal, and
-// dot_gq of the next L1 reuses dot_gkqk of L2) and uses three barriers per
-// iteration, one after each of L1 | L2 | L3 of cg_precond_jacobi.c:50-74.
+// dot_gq of the next L1 reuses dot_gkqk of L2), leaves the scalar
+// recurrences to thread 0 and the cross-thread sums to warp 0, and uses
+// three barriers per iteration, one after each of L1 | L2 | L3 of
+// cg_precond_jacobi.c:50-74.
 // The stop test uses the current gradient norm, not nbots' lagged one.
 #include <cstdint>
 
@@ -31,8 +33,13 @@ struct CgBsrArgs {
 };
 
 __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f64(CgBsrArgs a) {
-    __shared__ double red[3 * 32];
-    __shared__ double bc[3];
+    __shared__ double buf[3 * kPersistThreads];
+    __shared__ double s_coef;  // alpha, then beta
+    __shared__ int s_stop;
+    __shared__ struct {
+        double gq, gg, bb, target2;
+        uint32_t k;
+    } sc;  // scalar state, thread 0 only
     const unsigned G = gridDim.x;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nw = kPersistThreads / 32;
@@ -46,7 +53,14 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
     double2* __restrict__ w = reinterpret_cast<double2*>(a.w);
     const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
     const double2* __restrict__ dinv = reinterpret_cast<const double2*>(a.A.dinv64);
+    double* const part0 = a.part;
+    double* const part1 = a.part + kMaxBlocks;
+    double* const part2 = a.part + 3 * kMaxBlocks;  // own slot: L1 may overwrite [0, G) early
 
+    if (threadIdx.x == 0) {
+        sc.gq = sc.gg = sc.bb = sc.target2 = 0.0;
+        sc.k = 0;
+    }
     {   // init: g = A x - b, q = g / Aii, p = -q
         double v[3] = {0.0, 0.0, 0.0};  // gq, gg, bb
         for (uint32_t s = s0 + warp; s < s1; s += nw) {
@@ -63,20 +77,25 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
             v[1] = fma(gi.x, gi.x, fma(gi.y, gi.y, v[1]));
             v[2] = fma(bi.x, bi.x, fma(bi.y, bi.y, v[2]));
         }
-        publish<3>(v, red, a.part + 3 * kMaxBlocks);  // own slot: L1 may overwrite [0, G) early
+        double t[3];
+        block_sum_f64<3>(v, buf, t);
+        if (threadIdx.x == 0)
+            for (int j = 0; j < 3; j++) part2[blockIdx.x * 3 + j] = t[j];
     }
-    uint32_t k = 0;
-    double gq = 0.0, gg = 0.0, bb = 0.0, target2 = 0.0;
-    if (grid_barrier(a.bar, G, a.status)) goto done;
+    if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
     {
         double t[3];
-        grid_reduce<3>(a.part + 3 * kMaxBlocks, t, bc);
-        gq = t[0];
-        gg = t[1];
-        bb = t[2];
+        group_reduce0<3>(part2, G, t);
+        if (threadIdx.x == 0) {
+            sc.gq = t[0];
+            sc.gg = t[1];
+            sc.bb = t[2];
+            sc.target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * sc.bb : a.tol * a.tol;
+            s_stop = !(sc.gg > sc.target2) || a.max_iter == 0;
+        }
+        __syncthreads();
     }
-    target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * bb : a.tol * a.tol;
-    while (gg > target2 && k < a.max_iter) {
+    while (!s_stop) {
         {   // L1: w = A p, p.w
             double v[1] = {0.0};
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
@@ -87,13 +106,19 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
                 const double2 pi = p[i];
                 v[0] = fma(pi.x, wi.x, fma(pi.y, wi.y, v[0]));
             }
-            publish<1>(v, red, a.part);
+            double t[1];
+            block_sum_f64<1>(v, buf, t);
+            if (threadIdx.x == 0) part0[blockIdx.x] = t[0];
         }
-        if (grid_barrier(a.bar, G, a.status)) goto done;
-        double pw;
-        grid_reduce<1>(a.part, &pw, bc);
-        const double alpha = gq / pw;
+        if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
+        {
+            double pw[1];
+            group_reduce0<1>(part0, G, pw);
+            if (threadIdx.x == 0) s_coef = sc.gq / pw[0];
+            __syncthreads();
+        }
         {   // L2: x += alpha p, g += alpha w, q = g / Aii
+            const double alpha = s_coef;
             double v[2] = {0.0, 0.0};
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane;
@@ -111,32 +136,45 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
                 v[0] = fma(gi.x, qi.x, fma(gi.y, qi.y, v[0]));
                 v[1] = fma(gi.x, gi.x, fma(gi.y, gi.y, v[1]));
             }
-            publish<2>(v, red, a.part + kMaxBlocks);
+            double t[2];
+            block_sum_f64<2>(v, buf, t);
+            if (threadIdx.x == 0) {
+                part1[blockIdx.x * 2] = t[0];
+                part1[blockIdx.x * 2 + 1] = t[1];
+            }
         }
-        if (grid_barrier(a.bar, G, a.status)) goto done;
-        double t2[2];
-        grid_reduce<2>(a.part + kMaxBlocks, t2, bc);
-        const double beta = t2[0] / gq;
-        gq = t2[0];
-        gg = t2[1];
-        k++;
-        if (!(gg > target2) || k >= a.max_iter) break;
-        // L3: p = -q + beta p
-        for (uint32_t s = s0 + warp; s < s1; s += nw) {
-            const uint32_t i = s * 32 + lane;
-            if (i >= Nn) continue;
-            const double2 qi = q[i], pi = p[i];
-            p[i] = make_double2(fma(beta, pi.x, -qi.x), fma(beta, pi.y, -qi.y));
+        if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
+        {
+            double t2[2];
+            group_reduce0<2>(part1, G, t2);
+            if (threadIdx.x == 0) {
+                s_coef = t2[0] / sc.gq;  // beta
+                sc.gq = t2[0];
+                sc.gg = t2[1];
+                sc.k++;
+                s_stop = !(sc.gg > sc.target2) || sc.k >= a.max_iter;
+            }
+            __syncthreads();
         }
-        if (grid_barrier(a.bar, G, a.status)) goto done;
+        if (s_stop) break;
+        {   // L3: p = -q + beta p
+            const double beta = s_coef;
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane;
+                if (i >= Nn) continue;
+                const double2 qi = q[i], pi = p[i];
+                p[i] = make_double2(fma(beta, pi.x, -qi.x), fma(beta, pi.y, -qi.y));
+            }
+        }
+        if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
     }
 done:
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        a.res[0] = (double)k;
+        a.res[0] = (double)sc.k;
         int st = ld_volatile(a.status);
-        a.res[1] = st != 0 ? (double)st : (gg > target2 ? 1.0 : 0.0);
-        a.res[2] = gg;
-        a.res[3] = bb;
+        a.res[1] = st != 0 ? (double)st : (sc.gg > sc.target2 ? 1.0 : 0.0);
+        a.res[2] = sc.gg;
+        a.res[3] = sc.bb;
     }
 }
 

@@ -54,34 +54,40 @@ __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volati
 // Spin limit of every device-side wait (nanoseconds of %globaltimer).
 constexpr uint64_t kSpinLimitNs = 2000000000ull;
 
-// Grid-wide barrier: bar[0] arrival count, bar[1] generation.  Requires all
-// blocks to be co-resident (cooperative launch).  Returns nonzero when the
-// caller must stop (timeout here or an error recorded by another block).
-__device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, int* status) {
+// Barrier over the `nblocks` co-resident blocks of a group (the whole grid,
+// or one system of a batched launch), one arrival word *bar (zero at launch).
+// Thread 0 of the block of rank 0 adds 2^31 - (nblocks - 1), every other
+// block adds 1, each with one release atomic; the word has then grown by
+// exactly 2^31 once all have arrived, so each block waits (acquire loads)
+// for bit 31 to differ from the value its own atomic returned.  No reset is
+// needed between barriers.  Requires co-residency (cooperative launch).
+// The wait is bounded (kSpinLimitNs, checked every 64 polls).  Returns
+// nonzero when the caller must stop (timeout here or an error recorded by
+// another block).
+__device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, unsigned rank,
+                                            int* status) {
     __shared__ int s_stop;
     __syncthreads();
     if (threadIdx.x == 0) {
         int stop = 0;
-        unsigned gen = ld_acquire(&bar[1]);
-        // arrival: one acquire-release atomic publishes this block's writes
-        unsigned prev;
-        asm volatile("atom.add.acq_rel.gpu.global.u32 %0, [%1], 1;"
-                     : "=r"(prev)
-                     : "l"(&bar[0])
+        const unsigned add = rank == 0 ? 0x80000000u - (nblocks - 1) : 1u;
+        unsigned old;
+        asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;"
+                     : "=r"(old)
+                     : "l"(bar), "r"(add)
                      : "memory");
-        if (prev == nblocks - 1) {
-            // nobody touches the count again before the generation moves
-            asm volatile("st.relaxed.gpu.global.u32 [%0], 0;" ::"l"(&bar[0]) : "memory");
-            st_release(&bar[1], gen + 1);
-        } else {
-            uint64_t t0 = globaltimer();
-            while (ld_acquire(&bar[1]) == gen) {
-                if (globaltimer() - t0 > kSpinLimitNs) {
+        uint64_t t0 = 0;
+        for (unsigned it = 0;; it++) {
+            if ((ld_acquire(bar) ^ old) & 0x80000000u) break;
+            if ((it & 63u) == 0) {
+                const uint64_t t = globaltimer();
+                if (it == 0) {
+                    t0 = t;
+                } else if (t - t0 > kSpinLimitNs) {
                     atomicCAS(status, 0, NBG_ERR_TIMEOUT);
                     stop = 1;
                     break;
                 }
-                __nanosleep(32);
             }
         }
         if (!stop && ld_volatile(status) != 0) stop = 1;

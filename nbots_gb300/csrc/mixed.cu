@@ -52,16 +52,20 @@ struct MixArgs {
     __nv_bfloat16* pl;
     float *r, *wh, *xh, *xl;  // own-row vectors when they do not fit in shared memory
     __nv_bfloat16* wl;
-    double* part;  // L1 [0,K), L2 [K,3K), init/update [3K,6K), K = pstride
-    unsigned* bar;
-    int* status;
-    double* res;  // niter, updates, status, rr64, bb, b.u
     uint32_t max_iter;
     double tol, delta;
     unsigned flags;
-    int resident;             // own-row vectors live in shared memory
-    uint32_t s_begin, s_end;  // this system's slices
-    uint32_t g_base, g_size;  // this system's blocks in the launch
+    int resident;  // own-row vectors live in shared memory
+};
+
+// One system of a launch: its slices, its blocks and its synchronisation.
+struct Group {
+    double* part;  // L1 [0,K), L2 [K,3K), init/update [3K,6K), K = pstride
+    unsigned* bar;
+    int* status;
+    double* res;              // niter, updates, status, rr64, bb, b.u
+    uint32_t s_begin, s_end;  // slices
+    uint32_t g_base, g_size;  // blocks [g_base, g_base + g_size) of the launch
     uint32_t pstride;
 };
 
@@ -69,18 +73,26 @@ __device__ __forceinline__ float bf_round(float x) {
     return __bfloat162float(__float2bfloat16_rn(x));
 }
 
-// w = A p for node row (s, lane), split-precision operands, float-float sum
-__device__ __forceinline__ void spmv_row_split(const MixArgs& a, uint32_t s, uint32_t lane,
-                                               FF& y0, FF& y1) {
+// Half of w = A p for node row (s, r): lanes l and l + 16 share row
+// r = 16 h + (l & 15) of slice s, taking alternate entries, so a warp works on
+// half a slice at a time (the block's 2 (s1 - s0) half slices spread evenly
+// over its warps) and each load still covers two 16-entry runs.  The two
+// partial float-float sums are combined with one exchange; TwoSum is
+// symmetric, so both lanes hold the same bits.  Every lane of the warp must
+// call it (the exchange is warp-wide).
+__device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, uint32_t r,
+                                                uint32_t par, bool live, FF& y0, FF& y1) {
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
     const float2* __restrict__ ph = reinterpret_cast<const float2*>(a.ph);
     const __nv_bfloat162* __restrict__ pl = reinterpret_cast<const __nv_bfloat162*>(a.pl);
     FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
-    const uint32_t k0 = a.A.slice_off[s], k1 = a.A.slice_off[s + 1];
+    // rows past Nn in the last slice hold no entries: such lanes only
+    // take part in the exchange
+    const uint32_t k0 = a.A.slice_off[s] + par, k1 = live ? a.A.slice_off[s + 1] : 0;
 #pragma unroll 3
-    for (uint32_t k = k0; k < k1; k++) {
-        const size_t e = (size_t)k * 32 + lane;
+    for (uint32_t k = k0; k < k1; k += 2) {
+        const size_t e = (size_t)k * 32 + r;
         const uint32_t c = a.A.bcol[e];
         const float4 m = bh[e];
         const float4 ml = ulp16_decode4(bl[e], m);
@@ -91,8 +103,15 @@ __device__ __forceinline__ void spmv_row_split(const MixArgs& a, uint32_t s, uin
         c1.fma2(m.z, ml.z, pc.x, pcl.x);
         c1.fma2(m.w, ml.w, pc.y, pcl.y);
     }
-    y0 = c0.result();
-    y1 = c1.result();
+    FF t[2] = {c0.result(), c1.result()};
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const float h = __shfl_xor_sync(0xffffffffu, t[j].hi, 16);
+        const float l = __shfl_xor_sync(0xffffffffu, t[j].lo, 16);
+        t[j] = ff_add(t[j], FF{h, l});
+    }
+    y0 = t[0];
+    y1 = t[1];
 }
 
 // Own-row vectors of this block, indexed by local node row
@@ -101,8 +120,6 @@ struct Own {
     float2 *xh, *xl, *r, *dv, *wh, *ph;
     __nv_bfloat162 *wl, *pl;
 };
-
-__device__ __forceinline__ size_t own_smem_bytes(uint32_t nrows) { return (size_t)nrows * 56; }
 
 __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem, uint32_t s0,
                                            uint32_t nrows) {
@@ -168,27 +185,40 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
 }
 
 // The solver of one system on the blocks [g_base, g_base + g_size) of the
-// launch: its own slices, group barrier, partial sums and result.
-__device__ __forceinline__ void mixed_solve(const MixArgs& a, unsigned char* smem) {
+// launch: its own slices, group barrier, partial sums and result.  The
+// scalar recurrences (step lengths, residual norms, stopping and update
+// decisions) run in thread 0 in FP64 and reach the block through shared
+// memory as FP32 pairs and flags.
+__device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, unsigned char* smem) {
     __shared__ double red[3 * 32];
-    __shared__ double bc[3];
-    const unsigned G = a.g_size;
-    const uint32_t rank = blockIdx.x - a.g_base;
+    float2* const ffred = reinterpret_cast<float2*>(red);
+    __shared__ float s_alpha[2], s_beta[2];
+    __shared__ int s_flag;  // 0 iterate, 1 reliable update, 2 stop
+    __shared__ struct {
+        double rz, rmax2, rr64, bb, target2;
+        uint32_t k, nupd;
+        int converged;
+    } sc;  // scalar state, thread 0 only
+    const unsigned G = g.g_size;
+    const uint32_t rank = blockIdx.x - g.g_base;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     const uint32_t nw = kPersistThreads / 32;
     uint32_t s0, s1;
-    group_slice_range(a.s_begin, a.s_end, rank, G, s0, s1);
+    group_slice_range(g.s_begin, g.s_end, rank, G, s0, s1);
     const uint32_t Nn = a.A.Nn;
     const Own o = own_vectors(a, smem, s0, (s1 - s0) * 32);
     float2* __restrict__ gph = reinterpret_cast<float2*>(a.ph);
     __nv_bfloat162* __restrict__ gpl = reinterpret_cast<__nv_bfloat162*>(a.pl);
-    double* const part0 = a.part;
-    double* const part1 = a.part + a.pstride;
-    double* const part2 = a.part + 3 * a.pstride;
+    double* const part0 = g.part;
+    double* const part1 = g.part + g.pstride;
+    double* const part2 = g.part + 3 * g.pstride;
+    auto sync = [&]() { return grid_barrier(g.bar, G, rank, g.status); };
 
-    uint32_t k = 0, nupd = 0;
-    double rr64 = 0.0, bb = 0.0, target2 = 0.0, rz = 0.0, rr = 0.0, rmax2 = 0.0;
-    int converged = 0;
+    if (threadIdx.x == 0) {
+        sc.rz = sc.rmax2 = sc.rr64 = sc.bb = sc.target2 = 0.0;
+        sc.k = sc.nupd = 0;
+        sc.converged = 0;
+    }
     {   // init: own copy of 1/Aii, x = 0, r = b - A u (FP64), p = z
         const float2* __restrict__ gdv = reinterpret_cast<const float2*>(a.A.dinv32);
         for (uint32_t s = s0 + warp; s < s1; s += nw) {
@@ -206,112 +236,146 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, unsigned char* sme
         double v[3] = {rrl, bbl, (double)t.hi + (double)t.lo};
         group_publish<3>(v, red, part2, rank);
     }
-    if (grid_barrier(a.bar, G, a.status)) goto done;
+    if (sync()) goto done;
     {
         double t[3];
-        group_reduce<3>(part2, G, t, bc);
-        rr64 = t[0];
-        bb = t[1];
-        rz = t[2];
+        group_reduce0<3>(part2, G, t);
+        if (threadIdx.x == 0) {
+            sc.rr64 = t[0];
+            sc.bb = t[1];
+            sc.rz = t[2];
+            sc.target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * sc.bb : a.tol * a.tol;
+            sc.rmax2 = sc.rr64;
+            sc.converged = !(sc.rr64 > sc.target2);
+            s_flag = (sc.converged || a.max_iter == 0) ? 2 : 0;
+        }
+        __syncthreads();
     }
-    target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * bb : a.tol * a.tol;
-    rr = rmax2 = rr64;
-    converged = !(rr64 > target2);
-    {
-        const double d2 = a.delta * a.delta;
-        while (!converged && k < a.max_iter) {
-            {   // L1: w = A p, p.w
-                FFAcc pw{0.f, 0.f};
-                for (uint32_t s = s0 + warp; s < s1; s += nw) {
-                    const uint32_t i = s * 32 + lane, li = i - s0 * 32;
-                    if (i >= Nn) continue;
-                    FF y0, y1;
-                    spmv_row_split(a, s, lane, y0, y1);
-                    const float l0 = bf_round(y0.lo), l1 = bf_round(y1.lo);
-                    o.wh[li] = make_float2(y0.hi, y1.hi);
-                    o.wl[li] = __floats2bfloat162_rn(l0, l1);
-                    const float2 p = o.ph[li];
-                    const float2 plo = __bfloat1622float2(o.pl[li]);
-                    pw.fma2(p.x, plo.x, y0.hi, l0);
-                    pw.fma2(p.y, plo.y, y1.hi, l1);
-                }
-                const FF t = pw.result();
-                double v[1] = {(double)t.hi + (double)t.lo};
-                group_publish<1>(v, red, part0, rank);
+    while (s_flag != 2) {
+        {   // L1: w = A p, p.w (two lanes per node row)
+            FFAcc pw{0.f, 0.f};
+            const uint32_t par = lane >> 4;
+            for (uint32_t h = warp; h < 2 * (s1 - s0); h += nw) {
+                const uint32_t s = s0 + (h >> 1), r = ((h & 1) << 4) | (lane & 15);
+                const uint32_t i = s * 32 + r, li = i - s0 * 32;
+                // a slice's rows past Nn are padding: skip them whole (both lanes)
+                if (s * 32 + ((h & 1) << 4) >= Nn) continue;
+                FF y0, y1;
+                spmv_half_split(a, s, r, par, i < Nn, y0, y1);
+                if (par || i >= Nn) continue;
+                const float l0 = bf_round(y0.lo), l1 = bf_round(y1.lo);
+                o.wh[li] = make_float2(y0.hi, y1.hi);
+                o.wl[li] = __floats2bfloat162_rn(l0, l1);
+                const float2 p = o.ph[li];
+                const float2 plo = __bfloat1622float2(o.pl[li]);
+                pw.fma2(p.x, plo.x, y0.hi, l0);
+                pw.fma2(p.y, plo.y, y1.hi, l1);
             }
-            if (grid_barrier(a.bar, G, a.status)) goto done;
-            double pwd;
-            group_reduce<1>(part0, G, &pwd, bc);
-            const FF alpha = ff_from_double(rz / pwd);
-            {   // L2: x += alpha p, r -= alpha w, z = r / Aii (own rows only)
-                FFAcc rzk{0.f, 0.f}, rrk{0.f, 0.f};
-                for (uint32_t s = s0 + warp; s < s1; s += nw) {
-                    const uint32_t i = s * 32 + lane, li = i - s0 * 32;
-                    if (i >= Nn) continue;
-                    const float2 p = o.ph[li], plo = __bfloat1622float2(o.pl[li]);
-                    const float2 w = o.wh[li], wlo = __bfloat1622float2(o.wl[li]);
-                    const float2 xhi = o.xh[li], xlo = o.xl[li];
-                    const float2 ri = o.r[li], di = o.dv[li];
-                    const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, plo.x}));
-                    const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, plo.y}));
-                    o.xh[li] = make_float2(x0.hi, x1.hi);
-                    o.xl[li] = make_float2(x0.lo, x1.lo);
-                    const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
-                    const FF t0 = two_sum(ri.x, -aw0.hi), t1 = two_sum(ri.y, -aw1.hi);
-                    const float r0 = __fadd_rn(t0.hi, __fsub_rn(t0.lo, aw0.lo));
-                    const float r1 = __fadd_rn(t1.hi, __fsub_rn(t1.lo, aw1.lo));
-                    o.r[li] = make_float2(r0, r1);
-                    const FF z0 = two_prod(r0, di.x), z1 = two_prod(r1, di.y);
-                    rzk.fma2(r0, 0.f, z0.hi, z0.lo);
-                    rzk.fma2(r1, 0.f, z1.hi, z1.lo);
-                    rrk.fma2(r0, 0.f, r0, 0.f);
-                    rrk.fma2(r1, 0.f, r1, 0.f);
-                }
-                const FF t1 = rzk.result(), t2 = rrk.result();
-                double v[2] = {(double)t1.hi + (double)t1.lo, (double)t2.hi + (double)t2.lo};
-                group_publish<2>(v, red, part1, rank);
+            FF v[1] = {pw.result()};
+            group_publish_ff<1>(v, ffred, reinterpret_cast<float2*>(part0), rank);
+        }
+        if (sync()) goto done;
+        {
+            double pwd[1];
+            group_reduce0_ff<1>(reinterpret_cast<const float2*>(part0), G, pwd);
+            if (threadIdx.x == 0) {
+                const FF al = ff_from_double(sc.rz / pwd[0]);
+                s_alpha[0] = al.hi;
+                s_alpha[1] = al.lo;
             }
-            if (grid_barrier(a.bar, G, a.status)) goto done;
+            __syncthreads();
+        }
+        {   // L2: x += alpha p, r -= alpha w, z = r / Aii (own rows only)
+            const FF alpha = {s_alpha[0], s_alpha[1]};
+            FFAcc rzk{0.f, 0.f}, rrk{0.f, 0.f};
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane, li = i - s0 * 32;
+                if (i >= Nn) continue;
+                const float2 p = o.ph[li], plo = __bfloat1622float2(o.pl[li]);
+                const float2 w = o.wh[li], wlo = __bfloat1622float2(o.wl[li]);
+                const float2 xhi = o.xh[li], xlo = o.xl[li];
+                const float2 ri = o.r[li], di = o.dv[li];
+                const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, plo.x}));
+                const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, plo.y}));
+                o.xh[li] = make_float2(x0.hi, x1.hi);
+                o.xl[li] = make_float2(x0.lo, x1.lo);
+                const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
+                const FF t0 = two_sum(ri.x, -aw0.hi), t1 = two_sum(ri.y, -aw1.hi);
+                const float r0 = __fadd_rn(t0.hi, __fsub_rn(t0.lo, aw0.lo));
+                const float r1 = __fadd_rn(t1.hi, __fsub_rn(t1.lo, aw1.lo));
+                o.r[li] = make_float2(r0, r1);
+                const FF z0 = two_prod(r0, di.x), z1 = two_prod(r1, di.y);
+                rzk.fma2(r0, 0.f, z0.hi, z0.lo);
+                rzk.fma2(r1, 0.f, z1.hi, z1.lo);
+                rrk.fma2(r0, 0.f, r0, 0.f);
+                rrk.fma2(r1, 0.f, r1, 0.f);
+            }
+            FF v[2] = {rzk.result(), rrk.result()};
+            group_publish_ff<2>(v, ffred, reinterpret_cast<float2*>(part1), rank);
+        }
+        if (sync()) goto done;
+        {
             double t2[2];
-            group_reduce<2>(part1, G, t2, bc);
-            double rz_new = t2[0];
-            rr = t2[1];
-            if (rr > rmax2) rmax2 = rr;
-            k++;
-            if (rr <= d2 * rmax2 || rr <= target2 || k >= a.max_iter) {
-                // reliable update: u += x in FP64, then r = b - A u in FP64
-                double2* __restrict__ u = reinterpret_cast<double2*>(a.u);
-                for (uint32_t s = s0 + warp; s < s1; s += nw) {
-                    const uint32_t i = s * 32 + lane, li = i - s0 * 32;
-                    if (i >= Nn) continue;
-                    const float2 xhi = o.xh[li], xlo = o.xl[li];
-                    double2 ui = u[i];
-                    ui.x += (double)xhi.x + (double)xlo.x;
-                    ui.y += (double)xhi.y + (double)xlo.y;
-                    u[i] = ui;
-                    o.xh[li] = make_float2(0.f, 0.f);
-                    o.xl[li] = make_float2(0.f, 0.f);
+            group_reduce0_ff<2>(reinterpret_cast<const float2*>(part1), G, t2);
+            if (threadIdx.x == 0) {
+                const double rz_new = t2[0], rr = t2[1];
+                if (rr > sc.rmax2) sc.rmax2 = rr;
+                sc.k++;
+                const int upd = rr <= a.delta * a.delta * sc.rmax2 || rr <= sc.target2 ||
+                                sc.k >= a.max_iter;
+                if (!upd) {
+                    const FF be = ff_from_double(rz_new / sc.rz);
+                    sc.rz = rz_new;
+                    s_beta[0] = be.hi;
+                    s_beta[1] = be.lo;
                 }
-                if (grid_barrier(a.bar, G, a.status)) goto done;
-                double rrl = 0.0;
-                FFAcc rzk{0.f, 0.f};
-                true_residual(a, o, s0, s1, rrl, rzk, nullptr, false);
-                const FF t = rzk.result();
-                double v[2] = {rrl, (double)t.hi + (double)t.lo};
-                group_publish<2>(v, red, part2, rank);
-                if (grid_barrier(a.bar, G, a.status)) goto done;
-                double tt[2];
-                group_reduce<2>(part2, G, tt, bc);
-                rr64 = tt[0];
-                rz_new = tt[1];
-                rr = rmax2 = rr64;
-                nupd++;
-                converged = !(rr64 > target2);
-                if (converged || k >= a.max_iter) break;
+                s_flag = upd;
             }
-            const FF beta = ff_from_double(rz_new / rz);
-            rz = rz_new;
-            // L3: p = z + beta p (own copy and the global one)
+            __syncthreads();
+        }
+        if (s_flag) {
+            // reliable update: u += x in FP64, then r = b - A u in FP64
+            double2* __restrict__ u = reinterpret_cast<double2*>(a.u);
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane, li = i - s0 * 32;
+                if (i >= Nn) continue;
+                const float2 xhi = o.xh[li], xlo = o.xl[li];
+                double2 ui = u[i];
+                ui.x += (double)xhi.x + (double)xlo.x;
+                ui.y += (double)xhi.y + (double)xlo.y;
+                u[i] = ui;
+                o.xh[li] = make_float2(0.f, 0.f);
+                o.xl[li] = make_float2(0.f, 0.f);
+            }
+            if (sync()) goto done;
+            double rrl = 0.0;
+            FFAcc rzk{0.f, 0.f};
+            true_residual(a, o, s0, s1, rrl, rzk, nullptr, false);
+            const FF t = rzk.result();
+            double v[2] = {rrl, (double)t.hi + (double)t.lo};
+            group_publish<2>(v, red, part2, rank);
+            if (sync()) goto done;
+            double tt[2];
+            group_reduce0<2>(part2, G, tt);
+            if (threadIdx.x == 0) {
+                sc.rr64 = tt[0];
+                sc.rmax2 = sc.rr64;
+                sc.nupd++;
+                sc.converged = !(sc.rr64 > sc.target2);
+                const int stop = sc.converged || sc.k >= a.max_iter;
+                if (!stop) {
+                    const FF be = ff_from_double(tt[1] / sc.rz);
+                    sc.rz = tt[1];
+                    s_beta[0] = be.hi;
+                    s_beta[1] = be.lo;
+                }
+                s_flag = stop ? 2 : 0;
+            }
+            __syncthreads();
+            if (s_flag == 2) break;
+        }
+        {   // L3: p = z + beta p (own copy and the global one)
+            const FF beta = {s_beta[0], s_beta[1]};
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
@@ -328,8 +392,8 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, unsigned char* sme
                 gph[i] = hi;
                 gpl[i] = lo;
             }
-            if (grid_barrier(a.bar, G, a.status)) goto done;
         }
+        if (sync()) goto done;
     }
     {   // b.u in FP64 (the compliance F^T u when b is the load vector).  part0
         // was last read before the L2 barrier of the last iteration.
@@ -344,34 +408,38 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, unsigned char* sme
         }
         double v[1] = {bu};
         group_publish<1>(v, red, part0, rank);
-        if (grid_barrier(a.bar, G, a.status)) goto done;
-        group_reduce<1>(part0, G, &bu, bc);
-        if (rank == 0 && threadIdx.x == 0) a.res[5] = bu;
+        if (sync()) goto done;
+        double J[1];
+        group_reduce0<1>(part0, G, J);
+        if (rank == 0 && threadIdx.x == 0) g.res[5] = J[0];
     }
 done:
     if (rank == 0 && threadIdx.x == 0) {
-        a.res[0] = (double)k;
-        a.res[1] = (double)nupd;
-        int st = ld_volatile(a.status);
-        a.res[2] = st != 0 ? (double)st : (converged ? 0.0 : 1.0);
-        a.res[3] = rr64;
-        a.res[4] = bb;
+        g.res[0] = (double)sc.k;
+        g.res[1] = (double)sc.nupd;
+        int st = ld_volatile(g.status);
+        g.res[2] = st != 0 ? (double)st : (sc.converged ? 0.0 : 1.0);
+        g.res[3] = sc.rr64;
+        g.res[4] = sc.bb;
     }
 }
 
-__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed(MixArgs a) {
+__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed(MixArgs a,
+                                                                                Group g) {
     extern __shared__ __align__(16) unsigned char smem[];
-    mixed_solve(a, smem);
+    mixed_solve(a, g, smem);
 }
 
-// Many independent systems in one launch: block b solves many[block_of[b]].
+// Many independent systems stored in one block-diagonal layout, in one
+// launch: block b works for system groups[block_of[b]].
 __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
-    k_cg_mixed_many(const MixArgs* __restrict__ many, const uint32_t* __restrict__ block_of) {
+    k_cg_mixed_many(MixArgs a, const Group* __restrict__ groups,
+                    const uint32_t* __restrict__ block_of) {
     extern __shared__ __align__(16) unsigned char smem[];
-    __shared__ MixArgs sa;
-    if (threadIdx.x == 0) sa = many[block_of[blockIdx.x]];
+    __shared__ Group sg;
+    if (threadIdx.x == 0) sg = groups[block_of[blockIdx.x]];
     __syncthreads();
-    mixed_solve(sa, smem);
+    mixed_solve(a, sg, smem);
 }
 
 size_t mixed_bytes(uint32_t N) {
@@ -413,11 +481,12 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     a.xl = (float*)(base + 4 * f);
     a.pl = (__nv_bfloat16*)(base + 5 * f);
     a.wl = (__nv_bfloat16*)(base + 5 * f + h);
-    a.part = (double*)(base + 5 * f + 2 * h);
+    Group g;
+    g.part = (double*)(base + 5 * f + 2 * h);
     char* tail = base + 5 * f + 2 * h + align256(kMaxBlocks * 6 * 8);
-    a.bar = (unsigned*)tail;
-    a.status = (int*)(tail + 256);
-    a.res = (double*)(tail + 512);
+    g.bar = (unsigned*)tail;
+    g.status = (int*)(tail + 256);
+    g.res = (double*)(tail + 512);
     a.max_iter = max_iter;
     a.tol = tol;
     a.delta = delta;
@@ -431,18 +500,18 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
         rc = coop_grid_resident((const void*)k_cg_mixed, A->n_slices,
                                 NBG_MIXED_RESIDENT ? 56 * 32 : 0, &G, &dyn);
     a.resident = dyn > 0;
-    a.s_begin = 0;
-    a.s_end = A->n_slices;
-    a.g_base = 0;
-    a.g_size = G;
-    a.pstride = kMaxBlocks;
+    g.s_begin = 0;
+    g.s_end = A->n_slices;
+    g.g_base = 0;
+    g.g_size = G;
+    g.pstride = kMaxBlocks;
     if (e == cudaSuccess && rc == NBG_OK) {
-        void* args[] = {&a};
+        void* args[] = {&a, &g};
         e = cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(G), dim3(kPersistThreads),
                                         args, dyn, s);
     }
     if (e == cudaSuccess && rc == NBG_OK)
-        e = cudaMemcpyAsync(hr, a.res, sizeof(hr), cudaMemcpyDeviceToHost, s);
+        e = cudaMemcpyAsync(hr, g.res, sizeof(hr), cudaMemcpyDeviceToHost, s);
     if (e == cudaSuccess && rc == NBG_OK) e = cudaStreamSynchronize(s);
     if (e != cudaSuccess) rc = nbg_cuda_error(e);
     if (rc == NBG_OK) {
@@ -474,7 +543,8 @@ struct nbg_mixed_batch {
     unsigned flags;
     cudaStream_t stream;
     void* ws;
-    MixArgs* d_args;
+    MixArgs args;  // settings shared by every system
+    Group* d_groups;
     uint32_t* d_map;
     double* d_res;
     unsigned char* d_state;
@@ -499,7 +569,7 @@ constexpr size_t kResStride = 8;      // doubles of result per system
 
 size_t batch_bytes(uint32_t N, uint32_t n_sys) {
     return mixed_bytes(N) + align256((size_t)n_sys * kStateStride) +
-           align256((size_t)n_sys * kResStride * 8) + align256((size_t)n_sys * sizeof(MixArgs)) +
+           align256((size_t)n_sys * kResStride * 8) + align256((size_t)n_sys * sizeof(Group)) +
            align256((size_t)kMaxBlocks * 4);
 }
 
@@ -514,7 +584,11 @@ void bind_vectors(MixArgs& a, char* base, uint32_t N) {
     a.xl = (float*)(base + 4 * f);
     a.pl = (__nv_bfloat16*)(base + 5 * f);
     a.wl = (__nv_bfloat16*)(base + 5 * f + h);
-    a.part = (double*)(base + 5 * f + 2 * h);
+}
+
+double* part_slots(char* base, uint32_t N) {
+    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 2);
+    return (double*)(base + 5 * f + 2 * h);
 }
 
 // Blocks per system: one each, then one at a time to the system with the
@@ -601,36 +675,38 @@ int batch_plan(nbg_mixed_batch* m, double gamma) {
         for (uint32_t v : bl) G += v;
         dyn = 0;
     }
-    // argument table and block -> system map
-    std::vector<MixArgs> args(n);
-    std::vector<uint32_t> map(G);
+    // shared settings, group table and block -> system map
     char* base = (char*)m->ws;
-    unsigned g = 0;
+    MixArgs& a = m->args;
+    memset(&a, 0, sizeof(a));
+    a.A = m->A;
+    a.b = m->b;
+    a.u = m->x;
+    bind_vectors(a, base, m->A.N);
+    a.max_iter = m->max_iter;
+    a.tol = m->tol;
+    a.delta = m->delta;
+    a.flags = m->flags;
+    a.resident = dyn > 0;
+    std::vector<Group> groups(n);
+    std::vector<uint32_t> map(G);
+    double* part = part_slots(base, m->A.N);
+    unsigned gb = 0;
     for (uint32_t i = 0; i < n; i++) {
-        MixArgs& a = args[i];
-        memset(&a, 0, sizeof(a));
-        a.A = m->A;
-        a.b = m->b;
-        a.u = m->x;
-        bind_vectors(a, base, m->A.N);
-        a.part += 6 * (size_t)g;
-        a.pstride = bl[i];
-        a.bar = (unsigned*)(m->d_state + i * kStateStride);
-        a.status = (int*)(m->d_state + i * kStateStride + 128);
-        a.res = m->d_res + i * kResStride;
-        a.max_iter = m->max_iter;
-        a.tol = m->tol;
-        a.delta = m->delta;
-        a.flags = m->flags;
-        a.resident = dyn > 0;
-        a.s_begin = m->slice_ptr[i];
-        a.s_end = m->slice_ptr[i + 1];
-        a.g_base = g;
-        a.g_size = bl[i];
-        for (uint32_t k = 0; k < bl[i]; k++) map[g + k] = i;
-        g += bl[i];
+        Group& g = groups[i];
+        g.part = part + 6 * (size_t)gb;
+        g.pstride = bl[i];
+        g.bar = (unsigned*)(m->d_state + i * kStateStride);
+        g.status = (int*)(m->d_state + i * kStateStride + 128);
+        g.res = m->d_res + i * kResStride;
+        g.s_begin = m->slice_ptr[i];
+        g.s_end = m->slice_ptr[i + 1];
+        g.g_base = gb;
+        g.g_size = bl[i];
+        for (uint32_t k = 0; k < bl[i]; k++) map[gb + k] = i;
+        gb += bl[i];
     }
-    NBG_CHECK(cudaMemcpy(m->d_args, args.data(), n * sizeof(MixArgs), cudaMemcpyHostToDevice));
+    NBG_CHECK(cudaMemcpy(m->d_groups, groups.data(), n * sizeof(Group), cudaMemcpyHostToDevice));
     NBG_CHECK(cudaMemcpy(m->d_map, map.data(), G * 4, cudaMemcpyHostToDevice));
     m->blocks = bl;
     m->G = G;
@@ -655,9 +731,9 @@ cudaError_t batch_enqueue(nbg_mixed_batch* m, cudaStream_t s) {
     attr[0].val.cooperative = 1;
     cfg.attrs = attr;
     cfg.numAttrs = 1;
-    const MixArgs* args = m->d_args;
+    const Group* groups = m->d_groups;
     const uint32_t* map = m->d_map;
-    e = cudaLaunchKernelEx(&cfg, k_cg_mixed_many, args, map);
+    e = cudaLaunchKernelEx(&cfg, k_cg_mixed_many, m->args, groups, map);
     if (e != cudaSuccess || !m->sens) return e;
     const int rc = nbg_simp_sensitivity_f64(m->nen, m->N_elem, m->nod, m->conn, m->nu,
                                             m->thickness, m->rho, m->penal, m->E0, m->Emin, m->x,
@@ -736,8 +812,8 @@ extern "C" int nbg_mixed_batch_create(nbg_mixed_batch_t** out, const nbg_bsr_t* 
     p += align256((size_t)n_sys * kStateStride);
     m->d_res = (double*)p;
     p += align256((size_t)n_sys * kResStride * 8);
-    m->d_args = (MixArgs*)p;
-    p += align256((size_t)n_sys * sizeof(MixArgs));
+    m->d_groups = (Group*)p;
+    p += align256((size_t)n_sys * sizeof(Group));
     m->d_map = (uint32_t*)p;
     int rc = batch_plan(m, 1.0);
     if (rc != NBG_OK) {

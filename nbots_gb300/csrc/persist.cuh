@@ -121,6 +121,123 @@ __device__ __forceinline__ void group_reduce(const double* part, uint32_t G, dou
     __syncthreads();
 }
 
+// GB300 issues FP64 at a small fraction of its FP32 rate, so FP64 work that
+// every thread repeats (a shuffle tree over 512 threads, the division for a
+// step length) costs microseconds per reduction.  The helpers below keep the
+// per-thread part on the FP32 pipes and leave FP64 to one warp.
+
+// Block sum of NV float-float values per thread, error-free FP32 shuffle
+// sums throughout (within each warp, then across the warps by warp 0), fixed
+// order.  The result is valid in thread 0.  `scratch` holds NV * 32 FF.
+template <int NV>
+__device__ __forceinline__ void ff_warp_sum(FF (&v)[NV]) {
+#pragma unroll
+    for (int k = 0; k < NV; k++)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) {
+            const float h = __shfl_down_sync(0xffffffffu, v[k].hi, o);
+            const float l = __shfl_down_sync(0xffffffffu, v[k].lo, o);
+            v[k] = ff_add(v[k], FF{h, l});
+        }
+}
+
+template <int NV>
+__device__ __forceinline__ void block_sum_ff(FF (&v)[NV], float2* scratch) {
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const int nwarps = (blockDim.x + 31) >> 5;
+    ff_warp_sum<NV>(v);
+    __syncthreads();
+    if (lane == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) scratch[k * 32 + warp] = make_float2(v[k].hi, v[k].lo);
+    __syncthreads();
+    if (warp == 0) {
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            const float2 t = lane < nwarps ? scratch[k * 32 + lane] : make_float2(0.f, 0.f);
+            v[k] = FF{t.x, t.y};
+        }
+        ff_warp_sum<NV>(v);
+    }
+}
+
+// Block sum, then thread 0 stores the NV float-float results in this
+// block's slot of `part` (float2 per value).
+template <int NV>
+__device__ __forceinline__ void group_publish_ff(FF (&v)[NV], float2* scratch, float2* part,
+                                                 uint32_t rank) {
+    block_sum_ff<NV>(v, scratch);
+    if (threadIdx.x == 0)
+#pragma unroll
+        for (int k = 0; k < NV; k++) part[rank * NV + k] = make_float2(v[k].hi, v[k].lo);
+}
+
+// Sum over the group's blocks of NV float-float partials, in block order, by
+// warp 0 with error-free FP32 arithmetic; the result (as FP64) is valid in
+// thread 0 only (no block synchronisation).
+template <int NV>
+__device__ __forceinline__ void group_reduce0_ff(const float2* part, uint32_t G,
+                                                 double (&out)[NV]) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+        FF v[NV];
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            v[k] = FF{0.f, 0.f};
+            for (unsigned b = lane; b < G; b += 32) {
+                const float2 t = part[b * NV + k];
+                v[k] = ff_add(v[k], FF{t.x, t.y});
+            }
+        }
+        ff_warp_sum<NV>(v);
+#pragma unroll
+        for (int k = 0; k < NV; k++) out[k] = (double)v[k].hi + (double)v[k].lo;
+    }
+}
+
+// Block sum of NV FP64 values per thread with the FP64 adds done by warp 0
+// alone: the partials go through shared memory (`buf` holds NV * blockDim.x
+// doubles), lane l adds those of threads l, l + 32, ... in order, then a
+// shuffle tree.  About a quarter of the FP64 adds of a full-block shuffle
+// tree.  Result valid in thread 0.
+template <int NV>
+__device__ __forceinline__ void block_sum_f64(const double (&v)[NV], double* buf,
+                                              double (&out)[NV]) {
+    const int bd = blockDim.x;
+    __syncthreads();
+#pragma unroll
+    for (int k = 0; k < NV; k++) buf[k * bd + threadIdx.x] = v[k];
+    __syncthreads();
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (int t = lane; t < bd; t += 32) s += buf[k * bd + t];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            out[k] = s;
+        }
+    }
+}
+
+// Sum over the group's blocks of NV partials, in block order, by warp 0;
+// the result is valid in thread 0 only (no block synchronisation).
+template <int NV>
+__device__ __forceinline__ void group_reduce0(const double* part, uint32_t G, double (&out)[NV]) {
+    if (threadIdx.x < 32) {
+        const int lane = threadIdx.x;
+#pragma unroll
+        for (int k = 0; k < NV; k++) {
+            double s = 0.0;
+            for (unsigned b = lane; b < G; b += 32) s += part[b * NV + k];
+#pragma unroll
+            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
+            out[k] = s;
+        }
+    }
+}
+
 // (A x) for node row (s, lane) with FP64 values and FMAs.
 __device__ __forceinline__ double2 spmv_row_f64(const nbg_bsr_t& A, uint32_t s, uint32_t lane,
                                                 const double2* __restrict__ xv) {
