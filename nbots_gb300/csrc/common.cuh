@@ -54,6 +54,50 @@ __device__ __forceinline__ int ld_volatile(const int* p) { return *(const volati
 // Spin limit of every device-side wait (nanoseconds of %globaltimer).
 constexpr uint64_t kSpinLimitNs = 2000000000ull;
 
+// L2 eviction priority for streamed loads.  An iterative solver re-reads
+// the same matrix every iteration; when it is about as large as L2, plain
+// loads evict it in LRU order and every pass comes from HBM.  Marking a
+// fixed part of it evict_last (and the rest evict_first) keeps that part in
+// L2 from one iteration to the next.
+__device__ __forceinline__ uint64_t l2_policy(bool keep) {
+    uint64_t p;
+    if (keep)
+        asm volatile("createpolicy.fractional.L2::evict_last.b64 %0, 1.0;" : "=l"(p));
+    else
+        asm volatile("createpolicy.fractional.L2::evict_first.b64 %0, 1.0;" : "=l"(p));
+    return p;
+}
+
+__device__ __forceinline__ float4 ld_hint(const float4* a, uint64_t pol) {
+    float4 v;
+    asm volatile("ld.global.L2::cache_hint.v4.f32 {%0,%1,%2,%3}, [%4], %5;"
+                 : "=f"(v.x), "=f"(v.y), "=f"(v.z), "=f"(v.w)
+                 : "l"(a), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ double2 ld_hint(const double2* a, uint64_t pol) {
+    double2 v;
+    asm volatile("ld.global.L2::cache_hint.v2.f64 {%0,%1}, [%2], %3;"
+                 : "=d"(v.x), "=d"(v.y)
+                 : "l"(a), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ uint2 ld_hint(const uint2* a, uint64_t pol) {
+    uint2 v;
+    asm volatile("ld.global.L2::cache_hint.v2.u32 {%0,%1}, [%2], %3;"
+                 : "=r"(v.x), "=r"(v.y)
+                 : "l"(a), "l"(pol));
+    return v;
+}
+
+__device__ __forceinline__ uint32_t ld_hint(const uint32_t* a, uint64_t pol) {
+    uint32_t v;
+    asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
 // Barrier over the `nblocks` co-resident blocks of a group (the whole grid,
 // or one system of a batched launch), one arrival word *bar (zero at launch).
 // Thread 0 of the block of rank 0 adds 2^31 - (nblocks - 1), every other

@@ -41,6 +41,37 @@ using namespace nbg;
 #ifndef NBG_MIXED_RESIDENT
 #define NBG_MIXED_RESIDENT 1
 #endif
+#ifndef NBG_MIXED_UNROLL
+#define NBG_MIXED_UNROLL 4  // entries in flight per lane in the SpMV
+#endif
+// One 1024-thread block per SM: with two 512-thread blocks the SM serves one
+// block's warps first and the other block's SpMV ends several microseconds
+// later, which the next barrier then waits for.
+#ifndef NBG_MIXED_THREADS
+#define NBG_MIXED_THREADS 1024
+#endif
+#ifndef NBG_MIXED_MIN_BLOCKS
+#define NBG_MIXED_MIN_BLOCKS 1
+#endif
+constexpr int kMixThreads = NBG_MIXED_THREADS;
+constexpr int kMixMinBlocks = NBG_MIXED_MIN_BLOCKS;
+// Batched launches give every system at least one block, so they use
+// smaller blocks (more of them per SM) than the single-system launch.
+#ifndef NBG_BATCH_THREADS
+#define NBG_BATCH_THREADS 256
+#endif
+#ifndef NBG_BATCH_MIN_BLOCKS
+#define NBG_BATCH_MIN_BLOCKS 4
+#endif
+constexpr int kBatThreads = NBG_BATCH_THREADS;
+constexpr int kBatMinBlocks = NBG_BATCH_MIN_BLOCKS;
+constexpr int kUnroll = NBG_MIXED_UNROLL;
+#ifndef NBG_L2_KEEP
+#define NBG_L2_KEEP 50  // percent of L2 for the matrix part kept between iterations
+#endif
+#ifndef NBG_MIXED_PREFETCH
+#define NBG_MIXED_PREFETCH 0  // L2 bulk prefetch of upcoming slices in the SpMV
+#endif
 
 namespace {
 
@@ -55,7 +86,8 @@ struct MixArgs {
     uint32_t max_iter;
     double tol, delta;
     unsigned flags;
-    int resident;  // own-row vectors live in shared memory
+    int resident;      // own-row vectors live in shared memory
+    uint32_t keep_pm;  // per mille of each block's matrix stream kept in L2
 };
 
 // One system of a launch: its slices, its blocks and its synchronisation.
@@ -81,7 +113,8 @@ __device__ __forceinline__ float bf_round(float x) {
 // symmetric, so both lanes hold the same bits.  Every lane of the warp must
 // call it (the exchange is warp-wide).
 __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, uint32_t r,
-                                                uint32_t par, bool live, FF& y0, FF& y1) {
+                                                uint32_t par, bool live, uint64_t pol, FF& y0,
+                                                FF& y1) {
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
     const float2* __restrict__ ph = reinterpret_cast<const float2*>(a.ph);
@@ -90,12 +123,12 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     // rows past Nn in the last slice hold no entries: such lanes only
     // take part in the exchange
     const uint32_t k0 = a.A.slice_off[s] + par, k1 = live ? a.A.slice_off[s + 1] : 0;
-#pragma unroll 3
+#pragma unroll(kUnroll)
     for (uint32_t k = k0; k < k1; k += 2) {
         const size_t e = (size_t)k * 32 + r;
-        const uint32_t c = a.A.bcol[e];
-        const float4 m = bh[e];
-        const float4 ml = ulp16_decode4(bl[e], m);
+        const uint32_t c = ld_hint(a.A.bcol + e, pol);
+        const float4 m = ld_hint(bh + e, pol);
+        const float4 ml = ulp16_decode4(ld_hint(bl + e, pol), m);
         const float2 pc = ph[c];
         const float2 pcl = __bfloat1622float2(pl[c]);
         c0.fma2(m.x, ml.x, pc.x, pcl.x);
@@ -114,6 +147,24 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     y1 = t[1];
 }
 
+// Bring slice s's matrix stream (FP32 values, remainders, columns: one
+// contiguous range per array) into L2 with three bulk prefetches issued by
+// one lane.  The copy engine fetches ahead while the warp works on earlier
+// slices, so the SpMV's loads find L2 instead of waiting on HBM, without
+// holding registers.  Sizes are multiples of 128 B and starts 128 B-aligned.
+__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
+    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
+}
+
+__device__ __forceinline__ void prefetch_slice(const nbg_bsr_t& A, uint32_t s) {
+    const uint32_t k0 = A.slice_off[s], n = A.slice_off[s + 1] - k0;
+    if (n == 0) return;
+    const size_t e0 = (size_t)k0 * 32;
+    l2_prefetch(A.b32 + 4 * e0, n * 32 * 16);
+    l2_prefetch(A.blo + 4 * e0, n * 32 * 8);
+    l2_prefetch(A.bcol + e0, n * 32 * 4);
+}
+
 // Own-row vectors of this block, indexed by local node row
 // (i - 32 * s0): shared memory when they fit, else the global workspace.
 struct Own {
@@ -121,11 +172,12 @@ struct Own {
     __nv_bfloat162 *wl, *pl;
 };
 
+template <bool kRes>
 __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem, uint32_t s0,
                                            uint32_t nrows) {
     Own o;
     const size_t base = (size_t)s0 * 32;
-    if (a.resident) {
+    if (kRes) {
         float2* f = reinterpret_cast<float2*>(smem);
         o.xh = f;
         o.xl = f + nrows;
@@ -152,11 +204,12 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
 // r = b - A u in FP64 for the own rows, stored as FP32; z = r / Aii
 // (float-float); accumulates |r|^2 (FP64), r.z and optionally |b|^2; with
 // set_p, p = z (own copy and the global one).
+template <int kThreads>
 __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, uint32_t s0,
                                               uint32_t s1, double& rr, FFAcc& rz, double* bb,
                                               bool set_p) {
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t nw = kPersistThreads / 32;
+    const uint32_t nw = kThreads / 32;
     const double2* __restrict__ u = reinterpret_cast<const double2*>(a.u);
     const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
     for (uint32_t s = s0 + warp; s < s1; s += nw) {
@@ -189,6 +242,7 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
 // scalar recurrences (step lengths, residual norms, stopping and update
 // decisions) run in thread 0 in FP64 and reach the block through shared
 // memory as FP32 pairs and flags.
+template <bool kRes, int kThreads>
 __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, unsigned char* smem) {
     __shared__ double red[3 * 32];
     float2* const ffred = reinterpret_cast<float2*>(red);
@@ -202,11 +256,11 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     const unsigned G = g.g_size;
     const uint32_t rank = blockIdx.x - g.g_base;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
-    const uint32_t nw = kPersistThreads / 32;
+    const uint32_t nw = kThreads / 32;
     uint32_t s0, s1;
     group_slice_range(g.s_begin, g.s_end, rank, G, s0, s1);
     const uint32_t Nn = a.A.Nn;
-    const Own o = own_vectors(a, smem, s0, (s1 - s0) * 32);
+    const Own o = own_vectors<kRes>(a, smem, s0, (s1 - s0) * 32);
     float2* __restrict__ gph = reinterpret_cast<float2*>(a.ph);
     __nv_bfloat162* __restrict__ gpl = reinterpret_cast<__nv_bfloat162*>(a.pl);
     double* const part0 = g.part;
@@ -224,14 +278,14 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
         for (uint32_t s = s0 + warp; s < s1; s += nw) {
             const uint32_t i = s * 32 + lane, li = i - s0 * 32;
             if (i >= Nn) continue;
-            if (a.resident) o.dv[li] = gdv[i];
+            if (kRes) o.dv[li] = gdv[i];
             o.xh[li] = make_float2(0.f, 0.f);
             o.xl[li] = make_float2(0.f, 0.f);
         }
         __syncwarp();
         double rrl = 0.0, bbl = 0.0;
         FFAcc rzk{0.f, 0.f};
-        true_residual(a, o, s0, s1, rrl, rzk, &bbl, true);
+        true_residual<kThreads>(a, o, s0, s1, rrl, rzk, &bbl, true);
         const FF t = rzk.result();
         double v[3] = {rrl, bbl, (double)t.hi + (double)t.lo};
         group_publish<3>(v, red, part2, rank);
@@ -254,14 +308,24 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     while (s_flag != 2) {
         {   // L1: w = A p, p.w (two lanes per node row)
             FFAcc pw{0.f, 0.f};
-            const uint32_t par = lane >> 4;
-            for (uint32_t h = warp; h < 2 * (s1 - s0); h += nw) {
+            const uint32_t par = lane >> 4, nh = 2 * (s1 - s0);
+            // warp w takes half slices w, w + nw, ...: the slices of the even
+            // warps' first two rounds are prefetched now, each later round's
+            // two rounds ahead
+            if (NBG_MIXED_PREFETCH && lane == 0 && !(warp & 1))
+                for (uint32_t h = warp; h < nh && h < warp + 2 * nw; h += nw)
+                    prefetch_slice(a.A, s0 + (h >> 1));
+            for (uint32_t h = warp; h < nh; h += nw) {
+                if (NBG_MIXED_PREFETCH && lane == 0 && !(warp & 1) && h + 2 * nw < nh)
+                    prefetch_slice(a.A, s0 + ((h + 2 * nw) >> 1));
                 const uint32_t s = s0 + (h >> 1), r = ((h & 1) << 4) | (lane & 15);
                 const uint32_t i = s * 32 + r, li = i - s0 * 32;
                 // a slice's rows past Nn are padding: skip them whole (both lanes)
                 if (s * 32 + ((h & 1) << 4) >= Nn) continue;
                 FF y0, y1;
-                spmv_half_split(a, s, r, par, i < Nn, y0, y1);
+                // the first keep_pm / 1000 of this block's slices stay in L2
+                const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
+                spmv_half_split(a, s, r, par, i < Nn, pol, y0, y1);
                 if (par || i >= Nn) continue;
                 const float l0 = bf_round(y0.lo), l1 = bf_round(y1.lo);
                 o.wh[li] = make_float2(y0.hi, y1.hi);
@@ -350,7 +414,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             if (sync()) goto done;
             double rrl = 0.0;
             FFAcc rzk{0.f, 0.f};
-            true_residual(a, o, s0, s1, rrl, rzk, nullptr, false);
+            true_residual<kThreads>(a, o, s0, s1, rrl, rzk, nullptr, false);
             const FF t = rzk.result();
             double v[2] = {rrl, (double)t.hi + (double)t.lo};
             group_publish<2>(v, red, part2, rank);
@@ -385,7 +449,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
                 const FF n1 = ff_add(two_prod(ri.y, di.y), ff_mul(beta, {p.y, plo.y}));
                 const float2 hi = make_float2(n0.hi, n1.hi);
                 const __nv_bfloat162 lo = __floats2bfloat162_rn(n0.lo, n1.lo);
-                if (a.resident) {
+                if (kRes) {
                     o.ph[li] = hi;
                     o.pl[li] = lo;
                 }
@@ -424,22 +488,41 @@ done:
     }
 }
 
-__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_mixed(MixArgs a,
+// kRes: the block's own-row vectors live in dynamic shared memory (known at
+// compile time, so their addresses are 32-bit shared ones).
+template <bool kRes>
+__global__ void __launch_bounds__(kMixThreads, kMixMinBlocks) k_cg_mixed(MixArgs a,
                                                                                 Group g) {
     extern __shared__ __align__(16) unsigned char smem[];
-    mixed_solve(a, g, smem);
+    mixed_solve<kRes, kMixThreads>(a, g, smem);
 }
 
 // Many independent systems stored in one block-diagonal layout, in one
 // launch: block b works for system groups[block_of[b]].
-__global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks)
+template <bool kRes>
+__global__ void __launch_bounds__(kBatThreads, kBatMinBlocks)
     k_cg_mixed_many(MixArgs a, const Group* __restrict__ groups,
                     const uint32_t* __restrict__ block_of) {
     extern __shared__ __align__(16) unsigned char smem[];
     __shared__ Group sg;
     if (threadIdx.x == 0) sg = groups[block_of[blockIdx.x]];
     __syncthreads();
-    mixed_solve(a, sg, smem);
+    mixed_solve<kRes, kBatThreads>(a, sg, smem);
+}
+
+// Share of the SpMV's matrix stream (FP32 values, remainders, columns:
+// 28 B per block entry) marked evict_last: what fits in NBG_L2_KEEP percent
+// of this device's L2, the rest of L2 being left to the gathered vector and
+// the other data.
+uint32_t keep_permille(const nbg_bsr_t& A) {
+    int dev = 0, l2 = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess)
+        return 0;
+    const double stream = 28.0 * (double)A.n_entries;
+    const double budget = l2 * (NBG_L2_KEEP / 100.0);
+    if (stream <= 0.0 || budget >= stream) return 1000;
+    return (uint32_t)(1000.0 * budget / stream);
 }
 
 size_t mixed_bytes(uint32_t N) {
@@ -491,15 +574,20 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     a.tol = tol;
     a.delta = delta;
     a.flags = flags;
+    a.keep_pm = keep_permille(*A);
     int rc = NBG_OK;
     unsigned G = 1;
     size_t dyn = 0;
     double hr[5] = {0, 0, 0, 0, 0};
     cudaError_t e = cudaMemsetAsync(tail, 0, 3 * 256, s);
     if (e == cudaSuccess)
-        rc = coop_grid_resident((const void*)k_cg_mixed, A->n_slices,
-                                NBG_MIXED_RESIDENT ? 56 * 32 : 0, &G, &dyn);
+        rc = coop_grid_resident((const void*)k_cg_mixed<true>, A->n_slices,
+                                NBG_MIXED_RESIDENT ? 56 * 32 : 0, &G, &dyn, kMixThreads,
+                                kMixMinBlocks);
+    if (e == cudaSuccess && rc == NBG_OK && dyn == 0)
+        rc = coop_grid((const void*)k_cg_mixed<false>, A->n_slices, &G, kMixThreads);
     a.resident = dyn > 0;
+    const void* fn = a.resident ? (const void*)k_cg_mixed<true> : (const void*)k_cg_mixed<false>;
     g.s_begin = 0;
     g.s_end = A->n_slices;
     g.g_base = 0;
@@ -507,7 +595,7 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     g.pstride = kMaxBlocks;
     if (e == cudaSuccess && rc == NBG_OK) {
         void* args[] = {&a, &g};
-        e = cudaLaunchCooperativeKernel((const void*)k_cg_mixed, dim3(G), dim3(kPersistThreads),
+        e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kMixThreads),
                                         args, dyn, s);
     }
     if (e == cudaSuccess && rc == NBG_OK)
@@ -597,7 +685,7 @@ double* part_slots(char* base, uint32_t N) {
 void share_blocks(const std::vector<uint32_t>& sp, double gamma, unsigned total,
                   std::vector<uint32_t>& out) {
     const size_t n = sp.size() - 1;
-    const uint32_t nw = kPersistThreads / 32;
+    const uint32_t nw = kBatThreads / 32;
     std::vector<double> w(n);
     std::vector<uint32_t> cap(n);
     out.assign(n, 1);
@@ -637,7 +725,7 @@ void drop_graph(nbg_mixed_batch* m) {
 
 // Block shares, launch size and the per-system argument table for `gamma`.
 int batch_plan(nbg_mixed_batch* m, double gamma) {
-    const void* fn = (const void*)k_cg_mixed_many;
+    const void* fn = (const void*)k_cg_mixed_many<true>;
     int dev = 0, nsm = 0, optin = 0;
     NBG_CHECK(cudaGetDevice(&dev));
     NBG_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -649,7 +737,7 @@ int batch_plan(nbg_mixed_batch* m, double gamma) {
     unsigned G = 0;
     size_t dyn = 0;
     // own rows in shared memory when every block's rows fit
-    for (int per_sm = kPersistMinBlocks; NBG_MIXED_RESIDENT && per_sm >= 1 && !G; --per_sm) {
+    for (int per_sm = kBatMinBlocks; NBG_MIXED_RESIDENT && per_sm >= 1 && !G; --per_sm) {
         const unsigned total = std::min<unsigned>((unsigned)nsm * per_sm, kMaxBlocks);
         if (n > total) break;
         share_blocks(m->slice_ptr, gamma, total, bl);
@@ -657,7 +745,7 @@ int batch_plan(nbg_mixed_batch* m, double gamma) {
         if (bytes + fa.sharedSizeBytes > (size_t)optin) continue;
         NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         int occ = 0;
-        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, bytes));
+        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kBatThreads, bytes));
         unsigned used = 0;
         for (uint32_t v : bl) used += v;
         if ((unsigned)occ * (unsigned)nsm >= used) {
@@ -666,9 +754,9 @@ int batch_plan(nbg_mixed_batch* m, double gamma) {
         }
     }
     if (!G) {
-        NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 0));
+        fn = (const void*)k_cg_mixed_many<false>;
         int occ = 0;
-        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, 0));
+        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kBatThreads, 0));
         const unsigned total = std::min<unsigned>((unsigned)nsm * (unsigned)std::max(occ, 1), kMaxBlocks);
         if (n > total) return NBG_ERR_ARG;  // every system needs a co-resident block
         share_blocks(m->slice_ptr, gamma, total, bl);
@@ -687,6 +775,7 @@ int batch_plan(nbg_mixed_batch* m, double gamma) {
     a.tol = m->tol;
     a.delta = m->delta;
     a.flags = m->flags;
+    a.keep_pm = keep_permille(m->A);
     a.resident = dyn > 0;
     std::vector<Group> groups(n);
     std::vector<uint32_t> map(G);
@@ -723,7 +812,7 @@ cudaError_t batch_enqueue(nbg_mixed_batch* m, cudaStream_t s) {
     if (e != cudaSuccess) return e;
     cudaLaunchConfig_t cfg = {};
     cfg.gridDim = dim3(m->G);
-    cfg.blockDim = dim3(kPersistThreads);
+    cfg.blockDim = dim3(kBatThreads);
     cfg.dynamicSmemBytes = m->dyn;
     cfg.stream = s;
     cudaLaunchAttribute attr[1];
@@ -733,7 +822,8 @@ cudaError_t batch_enqueue(nbg_mixed_batch* m, cudaStream_t s) {
     cfg.numAttrs = 1;
     const Group* groups = m->d_groups;
     const uint32_t* map = m->d_map;
-    e = cudaLaunchKernelEx(&cfg, k_cg_mixed_many, m->args, groups, map);
+    e = m->args.resident ? cudaLaunchKernelEx(&cfg, k_cg_mixed_many<true>, m->args, groups, map)
+                         : cudaLaunchKernelEx(&cfg, k_cg_mixed_many<false>, m->args, groups, map);
     if (e != cudaSuccess || !m->sens) return e;
     const int rc = nbg_simp_sensitivity_f64(m->nen, m->N_elem, m->nod, m->conn, m->nu,
                                             m->thickness, m->rho, m->penal, m->E0, m->Emin, m->x,
@@ -744,8 +834,9 @@ cudaError_t batch_enqueue(nbg_mixed_batch* m, cudaStream_t s) {
 // The function attribute is shared by every batch in the process: set it
 // to this batch's size before capturing and before each replay.
 int set_smem(const nbg_mixed_batch* m) {
-    NBG_CHECK(cudaFuncSetAttribute((const void*)k_cg_mixed_many,
-                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->dyn));
+    if (m->args.resident)
+        NBG_CHECK(cudaFuncSetAttribute((const void*)k_cg_mixed_many<true>,
+                                       cudaFuncAttributeMaxDynamicSharedMemorySize, (int)m->dyn));
     return NBG_OK;
 }
 

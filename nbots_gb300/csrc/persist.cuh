@@ -184,6 +184,7 @@ __device__ __forceinline__ void group_reduce0_ff(const float2* part, uint32_t G,
 #pragma unroll
         for (int k = 0; k < NV; k++) {
             v[k] = FF{0.f, 0.f};
+#pragma unroll 8
             for (unsigned b = lane; b < G; b += 32) {
                 const float2 t = part[b * NV + k];
                 v[k] = ff_add(v[k], FF{t.x, t.y});
@@ -230,6 +231,7 @@ __device__ __forceinline__ void group_reduce0(const double* part, uint32_t G, do
 #pragma unroll
         for (int k = 0; k < NV; k++) {
             double s = 0.0;
+#pragma unroll 8
             for (unsigned b = lane; b < G; b += 32) s += part[b * NV + k];
 #pragma unroll
             for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
@@ -257,15 +259,16 @@ __device__ __forceinline__ double2 spmv_row_f64(const nbg_bsr_t& A, uint32_t s, 
     return make_double2(y0, y1);
 }
 
-// Grid size of a cooperative launch: every co-resident block, but not more
-// blocks than warps of slices.
-inline int coop_grid(const void* fn, uint32_t n_slices, unsigned* G) {
+// Grid size of a cooperative launch of `threads`-thread blocks: every
+// co-resident block, but not more blocks than warps of slices.
+inline int coop_grid(const void* fn, uint32_t n_slices, unsigned* G,
+                     int threads = kPersistThreads) {
     int dev = 0, nsm = 0, occ = 0;
     NBG_CHECK(cudaGetDevice(&dev));
     NBG_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-    NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, 0));
+    NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, 0));
     unsigned g = (unsigned)nsm * (unsigned)(occ > 0 ? occ : 1);
-    const unsigned want = (n_slices + kPersistThreads / 32 - 1) / (kPersistThreads / 32);
+    const unsigned want = (n_slices + threads / 32 - 1) / (threads / 32);
     if (want < g) g = want;
     if (g < 1) g = 1;
     if (g > kMaxBlocks) g = kMaxBlocks;
@@ -275,19 +278,20 @@ inline int coop_grid(const void* fn, uint32_t n_slices, unsigned* G) {
 
 // Grid of a persistent kernel whose blocks keep `bytes_per_slice` of own-row
 // data per slice in dynamic shared memory: the largest blocks-per-SM count
-// (kPersistMinBlocks, then 1) at which every block's slices fit.  *dyn = 0
+// (min_blocks, then fewer) at which every block's slices fit.  *dyn = 0
 // means they do not fit even at one block per SM and the kernel must keep
 // those rows in global memory.
 inline int coop_grid_resident(const void* fn, uint32_t n_slices, size_t bytes_per_slice,
-                              unsigned* G, size_t* dyn) {
+                              unsigned* G, size_t* dyn, int threads = kPersistThreads,
+                              int min_blocks = kPersistMinBlocks) {
     int dev = 0, nsm = 0, optin = 0;
     NBG_CHECK(cudaGetDevice(&dev));
     NBG_CHECK(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
     NBG_CHECK(cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev));
     cudaFuncAttributes fa;
     NBG_CHECK(cudaFuncGetAttributes(&fa, fn));
-    const unsigned want = (n_slices + kPersistThreads / 32 - 1) / (kPersistThreads / 32);
-    for (int per_sm = kPersistMinBlocks; bytes_per_slice && per_sm >= 1; --per_sm) {
+    const unsigned want = (n_slices + threads / 32 - 1) / (threads / 32);
+    for (int per_sm = min_blocks; bytes_per_slice && per_sm >= 1; --per_sm) {
         unsigned g = (unsigned)nsm * (unsigned)per_sm;
         if (want < g) g = want;
         if (g < 1) g = 1;
@@ -297,7 +301,7 @@ inline int coop_grid_resident(const void* fn, uint32_t n_slices, size_t bytes_pe
         NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize,
                                        (int)bytes));
         int occ = 0;
-        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kPersistThreads, bytes));
+        NBG_CHECK(cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, threads, bytes));
         if ((unsigned)occ * (unsigned)nsm >= g) {
             *G = g;
             *dyn = bytes;
@@ -306,7 +310,7 @@ inline int coop_grid_resident(const void* fn, uint32_t n_slices, size_t bytes_pe
     }
     *dyn = 0;
     NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, 0));
-    return coop_grid(fn, n_slices, G);
+    return coop_grid(fn, n_slices, G, threads);
 }
 
 }  // namespace nbg
