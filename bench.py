@@ -409,14 +409,23 @@ def run_gpu(args):
                            "frac": B_b32 / t_b32 / 1e9 / hbm, "bytes": B_b32},
             "peak_gbs": hbm, "peak_kind": peak_kind, "l2": "flushed before each launch"}
 
-    # ---- roofline of the mixed solver kernel: algorithmic bytes per iteration
-    # matrix: FP32 hi (16 B) + bf16 lo (8 B) + column (4 B) per 2x2 block;
-    # vectors: L1 12 B/dof, L2 40 B/dof, L3 20 B/dof (72 B/dof).
+    # ---- roofline of the mixed solver kernel: algorithmic bytes per iteration,
+    # counting each array the fused schedule moves through HBM once, in the
+    # format it reads.  Matrix stream per 2x2 block: FP32 values (16 B), 16-bit
+    # remainders (8 B), column (4 B), plus the slice offsets.  The block's own
+    # rows of x, r, w, p and 1/Aii live in shared memory for the whole solve;
+    # only the search direction p crosses HBM: written (FP32 + bf16 = 6 B/dof)
+    # in L3 and gathered (6 B/dof) by the next SpMV.  A reliable update reads
+    # the FP64 matrix (32 B values + 4 B column per block), u and b, writes u.
     it = r_mixed.niter
     t_med = float(np.median(t_mixed))
-    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 72 * N
-    upd_bytes = r_mixed.n_updates * (36 * nblk + 8 * N * 5)
+    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 12 * N
+    upd_bytes = (r_mixed.n_updates + 1) * (36 * nblk + 4 * (A.n_slices + 1) + 24 * N)
     achieved = (bytes_iter * it + upd_bytes) / t_med / 1e9
+    # fast FP64 kernel (vectors in global memory): 36 B per block, and per dof
+    # L1 p gather + own p + w (24 B), L2 p w 1/Aii x g in, x g q out (64 B),
+    # L3 q p in, p out (24 B)
+    fp64_bytes_iter = 36 * nblk + 4 * (A.n_slices + 1) + 112 * N
     traffic = None
     tpath = os.path.join(ROOT, "profiles", "mixed_cg_traffic.json")
     if os.path.exists(tpath):
@@ -489,7 +498,11 @@ def run_gpu(args):
                       "err_vs_fp64_rel_l2": err_vs_fp64},
             "fp64_gpu": {"s_per_solve": float(np.median(t_fp64)), "iters": r_fp64.niter,
                          "relres_fp64": rr_fp64,
-                         "us_per_iter": float(np.median(t_fp64)) / max(r_fp64.niter, 1) * 1e6},
+                         "us_per_iter": float(np.median(t_fp64)) / max(r_fp64.niter, 1) * 1e6,
+                         "bytes_per_iter": fp64_bytes_iter,
+                         "achieved_gbs": fp64_bytes_iter * r_fp64.niter /
+                                         float(np.median(t_fp64)) / 1e9,
+                         "bound": "fp64 issue (about 2 FP64 FMA per clock per SM on GB300)"},
             "nbots_order_fp64_gpu": {"s_per_solve": float(t_exact[0]), "iters": r_exact.niter},
             "speedup_mixed_vs_fp64_gpu": float(np.median(t_fp64)) / t_all,
             "setup_s": {"pattern_and_upload": t_create, "assembly_and_bcs": t_asm},
@@ -497,7 +510,10 @@ def run_gpu(args):
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
                          "traffic": traffic, "kernel": "k_cg_mixed",
-                         "bytes_per_iter": bytes_iter},
+                         "bytes_per_iter": bytes_iter,
+                         "note": "traffic is DRAM bytes per iteration from ncu; below "
+                                 "bytes_per_iter because part of the matrix stays in L2 "
+                                 "(evict_last) between iterations"},
             "e2e": {"value": e2e_all, "unit": "s",
                     "h2d_bytes_per_step": int(8 * nnz + 16 * N),
                     "d2h_bytes_per_step": int(8 * N),
@@ -507,6 +523,7 @@ def run_gpu(args):
             "c5_batch": c5,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
+            "dof_iters_per_s": N * it / t_all,
             "clocks": clk.summary(),
         }
         print(json.dumps(line))

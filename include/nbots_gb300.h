@@ -151,9 +151,9 @@ int nbg_cg_f64_noalloc(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_
  * (two rows per node with the same (2w, 2w+1) column pairs, sparse.c:36-52):
  * entry (slice s, k, lane r) sits at (slice_off[s] + k) * 32 + r; b64 holds
  * 4 doubles (a00 a01 a10 a11) per entry, b32 the same rounded to float and
- * blo the remainders (double - float) as signed 16-bit counts of
- * 2^-16 ulp(float), so that b32 + blo carries about 40 significant bits in
- * 6 bytes; dinv = 1 / diagonal per scalar row.  Any array may be NULL when a
+ * blo the remainders (double - float) as 16-bit counts q + 32768 of units
+ * of 2^-39 float (|q| <= 32767), so that b32 + blo carries about 40
+ * significant bits in 6 bytes; dinv = 1 / diagonal per scalar row.  Any array may be NULL when a
  * caller does not need it. */
 typedef struct {
     uint32_t N;            /* scalar rows (= 2 Nn) */

@@ -55,11 +55,11 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
         const float h00 = (float)a00, h01 = (float)a01, h10 = (float)a10, h11 = (float)a11;
         if (b32) reinterpret_cast<float4*>(b32)[e] = make_float4(h00, h01, h10, h11);
         if (blo) {
-            // remainders (exact in FP64) as 16-bit counts of 2^-16 ulp(hi)
-            const uint16_t q0 = (uint16_t)ulp16_encode(a00, h00);
-            const uint16_t q1 = (uint16_t)ulp16_encode(a01, h01);
-            const uint16_t q2 = (uint16_t)ulp16_encode(a10, h10);
-            const uint16_t q3 = (uint16_t)ulp16_encode(a11, h11);
+            // remainders (exact in FP64) as biased 16-bit counts of 2^-39 hi
+            const uint16_t q0 = rem16_encode(a00, h00);
+            const uint16_t q1 = rem16_encode(a01, h01);
+            const uint16_t q2 = rem16_encode(a10, h10);
+            const uint16_t q3 = rem16_encode(a11, h11);
             uint2 packed;
             packed.x = (uint32_t)q0 | ((uint32_t)q1 << 16);
             packed.y = (uint32_t)q2 | ((uint32_t)q3 << 16);

@@ -218,6 +218,16 @@ struct FFAcc {
         s = t.hi;
         c = __fadd_rn(c, __fadd_rn(t.lo, e));
     }
+    // (ahi + s ahi)(xhi + xlo) with the remainder given by its scale s
+    // (rem16_scale): the term s ahi xhi uses the rounded product ahi xhi.
+    __device__ __forceinline__ void fma2s(float ahi, float sc, float xhi, float xlo) {
+        FF p = two_prod(ahi, xhi);
+        float e = __fmaf_rn(ahi, xlo, p.lo);
+        e = __fmaf_rn(sc, p.hi, e);
+        FF t = two_sum(s, p.hi);
+        s = t.hi;
+        c = __fadd_rn(c, __fadd_rn(t.lo, e));
+    }
     __device__ __forceinline__ FF result() const { return fast_two_sum(s, c); }
 };
 
@@ -232,33 +242,34 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
     return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
-// Remainder of an FP32 rounding stored as a 16-bit integer count of
-// 2^-16 ulp(hi): hi + lo then carries about 40 significant bits in 6 bytes.
-// The unit 2^(E - 166) (E = biased exponent of hi) is built from bits; for
-// |hi| < 2^-87 the remainder is dropped.
-__device__ __forceinline__ float ulp16_unit(float hi) {
-    const int E = (int)((__float_as_uint(hi) >> 23) & 0xffu);
-    return E >= 40 ? __uint_as_float((uint32_t)(E - 39) << 23) : 0.f;
-}
-
-__device__ __forceinline__ int16_t ulp16_encode(double a, float hi) {
-    const float unit = ulp16_unit(hi);
-    if (unit == 0.f) return 0;
-    double q = rint((a - (double)hi) / (double)unit);
+// Remainder a - hi of an FP32 rounding hi = fl(a), stored in 16 bits as
+// the biased count q + 32768 of units of 2^-39 hi (|a - hi| <= 2^-24 |hi|,
+// so |q| <= 2^15, clamped to 32767): hi + lo then carries about 40
+// significant bits in 6 bytes.  Decoding needs no conversion instruction:
+// the count placed in the mantissa of a float with exponent -16 is
+// 2^-16 + (q + 32768) 2^-39, and subtracting 2^-16 + 2^-24 (exact) leaves
+// s = q 2^-39, with lo = s hi.
+__device__ __forceinline__ uint16_t rem16_encode(double a, float hi) {
+    if (hi == 0.f) return 32768;
+    double q = rint((a - (double)hi) / ((double)hi * 0x1p-39));
     q = q > 32767.0 ? 32767.0 : (q < -32767.0 ? -32767.0 : q);
-    return (int16_t)q;
+    return (uint16_t)((int)q + 32768);
 }
 
-__device__ __forceinline__ float ulp16_decode(int16_t q, float hi) {
-    return (float)q * ulp16_unit(hi);
+// s = q 2^-39 for the biased count in the low (hi16 = false) or high half
+// of v: one byte permute and one subtraction.
+__device__ __forceinline__ float rem16_scale(uint32_t v, bool hi16) {
+    uint32_t bits;
+    // bytes 0, 1 of the result from v's low or high half, bytes 2, 3 = 0x80, 0x37
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(bits) : "r"(v), "r"(0x37800000u),
+        "r"(hi16 ? 0x7632u : 0x7610u));
+    return __fsub_rn(__uint_as_float(bits), 0x1.01p-16f);
 }
 
-// The four remainders of one 2x2 block (packed 16-bit counts) as floats.
-__device__ __forceinline__ float4 ulp16_decode4(uint2 v, float4 hi) {
-    return make_float4(ulp16_decode((int16_t)(v.x & 0xffffu), hi.x),
-                       ulp16_decode((int16_t)(v.x >> 16), hi.y),
-                       ulp16_decode((int16_t)(v.y & 0xffffu), hi.z),
-                       ulp16_decode((int16_t)(v.y >> 16), hi.w));
+// The four scales of one 2x2 block (packed counts).
+__device__ __forceinline__ float4 rem16_scale4(uint2 v) {
+    return make_float4(rem16_scale(v.x, false), rem16_scale(v.x, true), rem16_scale(v.y, false),
+                       rem16_scale(v.y, true));
 }
 
 // a * b, both float-float

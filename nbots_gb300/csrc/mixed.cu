@@ -9,7 +9,7 @@
 // directions p and FP32 products A p, and an FP32 correction x.  The FP32
 // residual r is harmless.  So the inner iteration runs on the FP32 pipes
 // with:
-//   matrix      FP32 hi + a 16-bit remainder in units of 2^-16 ulp(hi)
+//   matrix      FP32 hi + a 16-bit remainder in units of 2^-39 hi
 //               (about 40 significant bits in 6 B/value instead of 8),
 //   p, A p      FP32 hi + bfloat16 lo per dof,
 //   x           float-float (FP32 hi + FP32 lo),
@@ -128,13 +128,13 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
         const size_t e = (size_t)k * 32 + r;
         const uint32_t c = ld_hint(a.A.bcol + e, pol);
         const float4 m = ld_hint(bh + e, pol);
-        const float4 ml = ulp16_decode4(ld_hint(bl + e, pol), m);
+        const float4 sc = rem16_scale4(ld_hint(bl + e, pol));
         const float2 pc = ph[c];
         const float2 pcl = __bfloat1622float2(pl[c]);
-        c0.fma2(m.x, ml.x, pc.x, pcl.x);
-        c0.fma2(m.y, ml.y, pc.y, pcl.y);
-        c1.fma2(m.z, ml.z, pc.x, pcl.x);
-        c1.fma2(m.w, ml.w, pc.y, pcl.y);
+        c0.fma2s(m.x, sc.x, pc.x, pcl.x);
+        c0.fma2s(m.y, sc.y, pc.y, pcl.y);
+        c1.fma2s(m.z, sc.z, pc.x, pcl.x);
+        c1.fma2s(m.w, sc.w, pc.y, pcl.y);
     }
     FF t[2] = {c0.result(), c1.result()};
 #pragma unroll

@@ -89,11 +89,11 @@ __global__ void __launch_bounds__(kWarps * 32, 1)
             const float2 pc = x2h[c];
             const float2 pcl = __bfloat1622float2(x2l[c]);
             const float4 m = mb[k * 32 + lane];
-            const float4 mlo = ulp16_decode4(ml[k * 32 + lane], m);
-            c0.fma2(m.x, mlo.x, pc.x, pcl.x);
-            c0.fma2(m.y, mlo.y, pc.y, pcl.y);
-            c1.fma2(m.z, mlo.z, pc.x, pcl.x);
-            c1.fma2(m.w, mlo.w, pc.y, pcl.y);
+            const float4 sc = rem16_scale4(ml[k * 32 + lane]);
+            c0.fma2s(m.x, sc.x, pc.x, pcl.x);
+            c0.fma2s(m.y, sc.y, pc.y, pcl.y);
+            c1.fma2s(m.z, sc.z, pc.x, pcl.x);
+            c1.fma2s(m.w, sc.w, pc.y, pcl.y);
         }
         const uint32_t i = s * 32 + lane;
         if (i < A.Nn) {
