@@ -268,6 +268,123 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush):
     return out
 
 
+def run_c3(args):
+    """The unstructured T3 L-shape (2M seeded points, about 4M dof): mesh
+    generation (host, not timed), pattern + upload, assembly + boundary
+    conditions, then mixed-precision and fast FP64 Jacobi-PCG to relres 1e-8
+    from u = 0 (CUDA events, L2 flushed before each solve), the mixed
+    solution's distance from the FP64 one, and a bounded sample of the
+    oracle's CPU iteration projected to the FP64 iteration count."""
+    import torch
+    from nbots_gb300 import _lib as L
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.fem import FemSystem
+    lib = L.lib()
+    dev = torch.device("cuda", 0)
+    stream = torch.cuda.current_stream(dev)
+    sp = C.c_void_p(stream.cuda_stream)
+    t0 = time.perf_counter()
+    p = W.config_c3()
+    t_gen = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    s = FemSystem(p, stream=sp)
+    t_create = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    assert s.assemble() == 0
+    s.apply_bcs()
+    A = s.block_layout()
+    torch.cuda.synchronize()
+    t_asm = time.perf_counter() - t0
+    N, nnz = s.N, s.nnz
+    F = s.dptr(L.FEM_F)
+    u = torch.zeros(N, dtype=torch.float64, device=dev)
+    ws_bytes = max(lib.nbg_cg_mixed_workspace_bytes(N), lib.nbg_cg_bsr_workspace_bytes(N))
+    ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
+    flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
+
+    def solve(kind):
+        u.zero_()
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        if kind == "mixed":
+            r = L.MixedResult()
+            rc = lib.nbg_cg_mixed(C.byref(A), F, u.data_ptr(), 8 * N, TOL, 0.1,
+                                  L.CG_JACOBI | L.CG_RELATIVE, C.byref(r), ws.data_ptr(),
+                                  ws_bytes, sp)
+        else:
+            r = L.CgResult()
+            rc = lib.nbg_cg_bsr_f64(C.byref(A), F, u.data_ptr(), 8 * N, TOL,
+                                    L.CG_JACOBI | L.CG_RELATIVE, C.byref(r), ws.data_ptr(),
+                                    ws_bytes, sp)
+        e1.record(stream)
+        e1.synchronize()
+        assert rc == 0 and r.status == 0, (kind, rc, r.status)
+        return e0.elapsed_time(e1) / 1e3, r
+    solve("mixed")
+    tm = [solve("mixed") for _ in range(max(1, args.steps))]
+    u_mixed = u.clone()
+    tf = [solve("fp64") for _ in range(max(1, min(args.steps, 2)))]
+    u_fp64 = u.clone()
+    Ft = torch.from_numpy(s.get(L.FEM_F)).to(dev)
+
+    def relres(x):
+        y = torch.empty(N, dtype=torch.float64, device=dev)
+        lib.nbg_spmv_bsr_f64(C.byref(A), x.data_ptr(), y.data_ptr(), sp)
+        torch.cuda.synchronize()
+        return float(torch.linalg.norm(Ft - y) / torch.linalg.norm(Ft))
+    t_mixed, r_mixed = min(tm, key=lambda x: x[0])
+    t_fp64, r_fp64 = min(tf, key=lambda x: x[0])
+    nblk = nnz // 4
+    # own rows do not fit in shared memory at this size, so besides the p
+    # exchange and 1/Aii (24 B/dof) they move through global memory: per node
+    # L1 w out, p in (16 + 16 B), L2 p, w, x, r in (16 + 16 + 16 + 8 B) and
+    # x, r out (16 + 8 B), L3 r, p in (8 + 16 B): 136 B
+    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 24 * N + 136 * (N // 2)
+    hbm, peak_kind = peaks()
+    cpu = None
+    if not args.no_cpu_baseline:
+        from oracle import oracle as O
+        threads = os.cpu_count() or 1
+        fl = O.Flat(p)
+        rp, ci = O.pattern(fl)
+        _, K, Fc = O.assemble(fl, rp, ci)
+        O.set_bconditions(fl, rp, ci, K, Fc)
+        O.cg_jacobi(rp, ci, K, Fc, max_iter=2, tol=0.0, threads=threads)
+        c0 = O.wtime()
+        O.cg_jacobi(rp, ci, K, Fc, max_iter=20, tol=0.0, threads=threads)
+        per_it = (O.wtime() - c0) / 20
+        cpu = {"value": per_it * r_fp64.niter, "unit": "s", "cores": threads, "kind": "port",
+               "sample": f"20 Jacobi-PCG iterations of the C oracle ({threads} threads), "
+                         f"{per_it * 1e3:.1f} ms/iteration, projected to the FP64 GPU "
+                         f"iteration count {r_fp64.niter}"}
+    line = {"workload": "C3: T3 L-shape [0,2]^2 minus (1,2]^2, 2M seeded uniform points + "
+                        "boundary points, Delaunay, Z-order numbering; E=1, nu=0.25, bottom "
+                        "clamped, unit +x traction on x=1, y in [1,2]; Jacobi-PCG to relres "
+                        "1e-8 from u=0",
+            "nodes": p.n_nodes, "triangles": p.n_elems, "dof": N, "nnz": nnz,
+            "block_entries": int(A.n_entries), "blocks": nblk,
+            "setup_s": {"mesh_generation_host": t_gen, "pattern_and_upload": t_create,
+                        "assembly_bcs_block_layout": t_asm},
+            "mixed": {"s_per_solve": t_mixed, "iters": r_mixed.niter,
+                      "updates": r_mixed.n_updates, "relres_fp64": relres(u_mixed),
+                      "us_per_iter": t_mixed / r_mixed.niter * 1e6,
+                      "err_vs_fp64_rel_l2": float(torch.linalg.norm(u_mixed - u_fp64) /
+                                                  torch.linalg.norm(u_fp64)),
+                      "bytes_per_iter": bytes_iter,
+                      "achieved_gbs": bytes_iter * r_mixed.niter / t_mixed / 1e9},
+            "fp64_gpu": {"s_per_solve": t_fp64, "iters": r_fp64.niter,
+                         "us_per_iter": t_fp64 / r_fp64.niter * 1e6,
+                         "relres_fp64": relres(u_fp64)},
+            "speedup_mixed_vs_fp64_gpu": t_fp64 / t_mixed,
+            "dof_iters_per_s_mixed": N * r_mixed.niter / t_mixed,
+            "peak_gbs": hbm, "peak_kind": peak_kind, "cpu_baseline": cpu}
+    print(json.dumps(line))
+    s.close()
+    return 0
+
+
 def run_gpu(args):
     import torch
     import torch.distributed as dist
@@ -413,13 +530,14 @@ def run_gpu(args):
     # counting each array the fused schedule moves through HBM once, in the
     # format it reads.  Matrix stream per 2x2 block: FP32 values (16 B), 16-bit
     # remainders (8 B), column (4 B), plus the slice offsets.  The block's own
-    # rows of x, r, w, p and 1/Aii live in shared memory for the whole solve;
-    # only the search direction p crosses HBM: written (FP32 + bf16 = 6 B/dof)
-    # in L3 and gathered (6 B/dof) by the next SpMV.  A reliable update reads
-    # the FP64 matrix (32 B values + 4 B column per block), u and b, writes u.
+    # rows of x, r, w and p live in shared memory for the whole solve; the
+    # search direction p crosses HBM (written as FP32 hi + lo, 8 B/dof, in L3
+    # and gathered, 8 B/dof, by the next SpMV) and 1/Aii (4 B/dof) is read in
+    # L2 and L3.  A reliable update reads the FP64 matrix (32 B values + 4 B
+    # column per block), u and b, writes u.
     it = r_mixed.niter
     t_med = float(np.median(t_mixed))
-    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 12 * N
+    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 24 * N
     upd_bytes = (r_mixed.n_updates + 1) * (36 * nblk + 4 * (A.n_slices + 1) + 24 * N)
     achieved = (bytes_iter * it + upd_bytes) / t_med / 1e9
     # fast FP64 kernel (vectors in global memory): 36 B per block, and per dof
@@ -598,6 +716,9 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c4", action="store_true", help="skip the SIMP gradient timings")
     ap.add_argument("--no-c5", action="store_true", help="skip the batched solves")
+    ap.add_argument("--c3", action="store_true",
+                    help="run the 4M-dof unstructured T3 L-shape instead (mesh generation "
+                         "takes about a minute on the host)")
     ap.add_argument("--profile", choices=["mixed", "fp64", "spmv"],
                     help="one bounded kernel launch for ncu instead of the benchmark")
     ap.add_argument("--iters", type=int, default=100)
@@ -606,6 +727,8 @@ def main():
         return run_profile(args)
     if args.impl == "reference":
         return run_reference(args)
+    if args.c3:
+        return run_c3(args)
     return run_gpu(args)
 
 

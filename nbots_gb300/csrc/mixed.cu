@@ -11,7 +11,7 @@
 // with:
 //   matrix      FP32 hi + a 16-bit remainder in units of 2^-39 hi
 //               (about 40 significant bits in 6 B/value instead of 8),
-//   p, A p      FP32 hi + bfloat16 lo per dof,
+//   p, A p      FP32 hi + FP32 lo per dof (float-float),
 //   x           float-float (FP32 hi + FP32 lo),
 //   r           FP32,
 // products and sums by error-free transformations (TwoProduct with FMA,
@@ -40,6 +40,15 @@ using namespace nbg;
 // (overridable at build time for tuning).
 #ifndef NBG_MIXED_RESIDENT
 #define NBG_MIXED_RESIDENT 1
+#endif
+// FP32 low parts for both p and A p: with bfloat16 ones (32 significant
+// bits) the 4M-dof unstructured T3 case needed 26,067 iterations against
+// FP64's 22,323; with FP32 ones 22,563.
+#ifndef NBG_MIXED_PLO32
+#define NBG_MIXED_PLO32 1
+#endif
+#ifndef NBG_MIXED_WLO32
+#define NBG_MIXED_WLO32 1
 #endif
 #ifndef NBG_MIXED_UNROLL
 #define NBG_MIXED_UNROLL 4  // entries in flight per lane in the SpMV
@@ -75,14 +84,54 @@ constexpr int kUnroll = NBG_MIXED_UNROLL;
 
 namespace {
 
+// Low parts of p and of A p: bfloat16 (FP32 hi + 8 bits) or FP32 (hi + lo
+// about 48 bits), chosen separately (NBG_MIXED_PLO32, NBG_MIXED_WLO32).
+struct LoBF {
+    using one = __nv_bfloat16;
+    using two = __nv_bfloat162;
+    static __device__ __forceinline__ two pack(float a, float b) {
+        return __floats2bfloat162_rn(a, b);
+    }
+    static __device__ __forceinline__ float2 unpack(two v) { return __bfloat1622float2(v); }
+    static __device__ __forceinline__ float round(float x) {
+        return __bfloat162float(__float2bfloat16_rn(x));
+    }
+};
+struct LoF32 {
+    using one = float;
+    using two = float2;
+    static __device__ __forceinline__ two pack(float a, float b) { return make_float2(a, b); }
+    static __device__ __forceinline__ float2 unpack(two v) { return v; }
+    static __device__ __forceinline__ float round(float x) { return x; }
+};
+#if NBG_MIXED_PLO32
+using LoP = LoF32;
+#else
+using LoP = LoBF;
+#endif
+#if NBG_MIXED_WLO32
+using LoW = LoF32;
+#else
+using LoW = LoBF;
+#endif
+// 1/Aii in shared memory too, or read from global memory (L2) when the
+// shared memory is better left to the L1 cache of the SpMV's gathers
+#ifndef NBG_MIXED_DV_SHARED
+#define NBG_MIXED_DV_SHARED 0
+#endif
+constexpr bool kDvShared = NBG_MIXED_DV_SHARED;
+// own-row bytes per node: x (hi, lo), r, A p hi, p hi (8 B each), 1/Aii
+// (8 B, when shared) and the low pairs
+constexpr size_t kOwnNodeBytes = 40 + (kDvShared ? 8 : 0) + sizeof(LoP::two) + sizeof(LoW::two);
+
 struct MixArgs {
     nbg_bsr_t A;
     const double* b;
     double* u;
     float* ph;               // search direction, global (gathered by neighbours)
-    __nv_bfloat16* pl;
+    LoP::one* pl;
     float *r, *wh, *xh, *xl;  // own-row vectors when they do not fit in shared memory
-    __nv_bfloat16* wl;
+    LoW::one* wl;
     uint32_t max_iter;
     double tol, delta;
     unsigned flags;
@@ -101,9 +150,7 @@ struct Group {
     uint32_t pstride;
 };
 
-__device__ __forceinline__ float bf_round(float x) {
-    return __bfloat162float(__float2bfloat16_rn(x));
-}
+
 
 // Half of w = A p for node row (s, r): lanes l and l + 16 share row
 // r = 16 h + (l & 15) of slice s, taking alternate entries, so a warp works on
@@ -118,7 +165,7 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
     const float2* __restrict__ ph = reinterpret_cast<const float2*>(a.ph);
-    const __nv_bfloat162* __restrict__ pl = reinterpret_cast<const __nv_bfloat162*>(a.pl);
+    const LoP::two* __restrict__ pl = reinterpret_cast<const LoP::two*>(a.pl);
     FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
     // rows past Nn in the last slice hold no entries: such lanes only
     // take part in the exchange
@@ -130,7 +177,7 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
         const float4 m = ld_hint(bh + e, pol);
         const float4 sc = rem16_scale4(ld_hint(bl + e, pol));
         const float2 pc = ph[c];
-        const float2 pcl = __bfloat1622float2(pl[c]);
+        const float2 pcl = LoP::unpack(pl[c]);
         c0.fma2s(m.x, sc.x, pc.x, pcl.x);
         c0.fma2s(m.y, sc.y, pc.y, pcl.y);
         c1.fma2s(m.z, sc.z, pc.x, pcl.x);
@@ -169,7 +216,8 @@ __device__ __forceinline__ void prefetch_slice(const nbg_bsr_t& A, uint32_t s) {
 // (i - 32 * s0): shared memory when they fit, else the global workspace.
 struct Own {
     float2 *xh, *xl, *r, *dv, *wh, *ph;
-    __nv_bfloat162 *wl, *pl;
+    LoW::two* wl;
+    LoP::two* pl;
 };
 
 template <bool kRes>
@@ -182,12 +230,17 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
         o.xh = f;
         o.xl = f + nrows;
         o.r = f + 2 * nrows;
-        o.dv = f + 3 * nrows;
-        o.wh = f + 4 * nrows;
-        o.ph = f + 5 * nrows;
-        __nv_bfloat162* h = reinterpret_cast<__nv_bfloat162*>(f + 6 * nrows);
-        o.wl = h;
-        o.pl = h + nrows;
+        o.wh = f + 3 * nrows;
+        o.ph = f + 4 * nrows;
+        f += 5 * nrows;
+        if (kDvShared) {
+            o.dv = f;
+            f += nrows;
+        } else {
+            o.dv = const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) + base;
+        }
+        o.wl = reinterpret_cast<LoW::two*>(f);
+        o.pl = reinterpret_cast<LoP::two*>(o.wl + nrows);
     } else {
         o.xh = reinterpret_cast<float2*>(a.xh) + base;
         o.xl = reinterpret_cast<float2*>(a.xl) + base;
@@ -195,8 +248,8 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
         o.dv = const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) + base;
         o.wh = reinterpret_cast<float2*>(a.wh) + base;
         o.ph = reinterpret_cast<float2*>(a.ph) + base;
-        o.wl = reinterpret_cast<__nv_bfloat162*>(a.wl) + base;
-        o.pl = reinterpret_cast<__nv_bfloat162*>(a.pl) + base;
+        o.wl = reinterpret_cast<LoW::two*>(a.wl) + base;
+        o.pl = reinterpret_cast<LoP::two*>(a.pl) + base;
     }
     return o;
 }
@@ -228,11 +281,11 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
         rz.fma2(f1, 0.f, z1.hi, z1.lo);
         if (set_p) {
             const float2 hi = make_float2(z0.hi, z1.hi);
-            const __nv_bfloat162 lo = __floats2bfloat162_rn(z0.lo, z1.lo);
+            const LoP::two lo = LoP::pack(z0.lo, z1.lo);
             o.ph[li] = hi;
             o.pl[li] = lo;
             reinterpret_cast<float2*>(a.ph)[i] = hi;
-            reinterpret_cast<__nv_bfloat162*>(a.pl)[i] = lo;
+            reinterpret_cast<LoP::two*>(a.pl)[i] = lo;
         }
     }
 }
@@ -262,7 +315,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     const uint32_t Nn = a.A.Nn;
     const Own o = own_vectors<kRes>(a, smem, s0, (s1 - s0) * 32);
     float2* __restrict__ gph = reinterpret_cast<float2*>(a.ph);
-    __nv_bfloat162* __restrict__ gpl = reinterpret_cast<__nv_bfloat162*>(a.pl);
+    LoP::two* __restrict__ gpl = reinterpret_cast<LoP::two*>(a.pl);
     double* const part0 = g.part;
     double* const part1 = g.part + g.pstride;
     double* const part2 = g.part + 3 * g.pstride;
@@ -278,7 +331,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
         for (uint32_t s = s0 + warp; s < s1; s += nw) {
             const uint32_t i = s * 32 + lane, li = i - s0 * 32;
             if (i >= Nn) continue;
-            if (kRes) o.dv[li] = gdv[i];
+            if (kRes && kDvShared) o.dv[li] = gdv[i];
             o.xh[li] = make_float2(0.f, 0.f);
             o.xl[li] = make_float2(0.f, 0.f);
         }
@@ -327,11 +380,11 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
                 const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
                 spmv_half_split(a, s, r, par, i < Nn, pol, y0, y1);
                 if (par || i >= Nn) continue;
-                const float l0 = bf_round(y0.lo), l1 = bf_round(y1.lo);
+                const float l0 = LoW::round(y0.lo), l1 = LoW::round(y1.lo);
                 o.wh[li] = make_float2(y0.hi, y1.hi);
-                o.wl[li] = __floats2bfloat162_rn(l0, l1);
+                o.wl[li] = LoW::pack(l0, l1);
                 const float2 p = o.ph[li];
-                const float2 plo = __bfloat1622float2(o.pl[li]);
+                const float2 plo = LoP::unpack(o.pl[li]);
                 pw.fma2(p.x, plo.x, y0.hi, l0);
                 pw.fma2(p.y, plo.y, y1.hi, l1);
             }
@@ -355,8 +408,8 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
-                const float2 p = o.ph[li], plo = __bfloat1622float2(o.pl[li]);
-                const float2 w = o.wh[li], wlo = __bfloat1622float2(o.wl[li]);
+                const float2 p = o.ph[li], plo = LoP::unpack(o.pl[li]);
+                const float2 w = o.wh[li], wlo = LoW::unpack(o.wl[li]);
                 const float2 xhi = o.xh[li], xlo = o.xl[li];
                 const float2 ri = o.r[li], di = o.dv[li];
                 const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, plo.x}));
@@ -444,11 +497,11 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
                 const float2 ri = o.r[li], di = o.dv[li];
-                const float2 p = o.ph[li], plo = __bfloat1622float2(o.pl[li]);
+                const float2 p = o.ph[li], plo = LoP::unpack(o.pl[li]);
                 const FF n0 = ff_add(two_prod(ri.x, di.x), ff_mul(beta, {p.x, plo.x}));
                 const FF n1 = ff_add(two_prod(ri.y, di.y), ff_mul(beta, {p.y, plo.y}));
                 const float2 hi = make_float2(n0.hi, n1.hi);
-                const __nv_bfloat162 lo = __floats2bfloat162_rn(n0.lo, n1.lo);
+                const LoP::two lo = LoP::pack(n0.lo, n1.lo);
                 if (kRes) {
                     o.ph[li] = hi;
                     o.pl[li] = lo;
@@ -526,7 +579,7 @@ uint32_t keep_permille(const nbg_bsr_t& A) {
 }
 
 size_t mixed_bytes(uint32_t N) {
-    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 2);
+    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
     return 5 * f + 2 * h + align256(kMaxBlocks * 6 * 8) + 3 * 256;
 }
 
@@ -552,7 +605,7 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
         return NBG_ERR_ARG;
     }
     char* base = (char*)ws;
-    const size_t f = align256((size_t)A->N * 4), h = align256((size_t)A->N * 2);
+    const size_t f = align256((size_t)A->N * 4), h = align256((size_t)A->N * 4);
     MixArgs a;
     a.A = *A;
     a.b = b;
@@ -562,8 +615,8 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     a.wh = (float*)(base + 2 * f);
     a.xh = (float*)(base + 3 * f);
     a.xl = (float*)(base + 4 * f);
-    a.pl = (__nv_bfloat16*)(base + 5 * f);
-    a.wl = (__nv_bfloat16*)(base + 5 * f + h);
+    a.pl = (LoP::one*)(base + 5 * f);
+    a.wl = (LoW::one*)(base + 5 * f + h);
     Group g;
     g.part = (double*)(base + 5 * f + 2 * h);
     char* tail = base + 5 * f + 2 * h + align256(kMaxBlocks * 6 * 8);
@@ -582,7 +635,7 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     cudaError_t e = cudaMemsetAsync(tail, 0, 3 * 256, s);
     if (e == cudaSuccess)
         rc = coop_grid_resident((const void*)k_cg_mixed<true>, A->n_slices,
-                                NBG_MIXED_RESIDENT ? 56 * 32 : 0, &G, &dyn, kMixThreads,
+                                NBG_MIXED_RESIDENT ? kOwnNodeBytes * 32 : 0, &G, &dyn, kMixThreads,
                                 kMixMinBlocks);
     if (e == cudaSuccess && rc == NBG_OK && dyn == 0)
         rc = coop_grid((const void*)k_cg_mixed<false>, A->n_slices, &G, kMixThreads);
@@ -664,18 +717,18 @@ size_t batch_bytes(uint32_t N, uint32_t n_sys) {
 // Vector slots of the workspace shared by every system (indexed by the
 // global node row).
 void bind_vectors(MixArgs& a, char* base, uint32_t N) {
-    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 2);
+    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
     a.r = (float*)base;
     a.ph = (float*)(base + f);
     a.wh = (float*)(base + 2 * f);
     a.xh = (float*)(base + 3 * f);
     a.xl = (float*)(base + 4 * f);
-    a.pl = (__nv_bfloat16*)(base + 5 * f);
-    a.wl = (__nv_bfloat16*)(base + 5 * f + h);
+    a.pl = (LoP::one*)(base + 5 * f);
+    a.wl = (LoW::one*)(base + 5 * f + h);
 }
 
 double* part_slots(char* base, uint32_t N) {
-    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 2);
+    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
     return (double*)(base + 5 * f + 2 * h);
 }
 
@@ -741,7 +794,7 @@ int batch_plan(nbg_mixed_batch* m, double gamma) {
         const unsigned total = std::min<unsigned>((unsigned)nsm * per_sm, kMaxBlocks);
         if (n > total) break;
         share_blocks(m->slice_ptr, gamma, total, bl);
-        const size_t bytes = (size_t)max_slices_per_block(m->slice_ptr, bl) * 56 * 32;
+        const size_t bytes = (size_t)max_slices_per_block(m->slice_ptr, bl) * kOwnNodeBytes * 32;
         if (bytes + fa.sharedSizeBytes > (size_t)optin) continue;
         NBG_CHECK(cudaFuncSetAttribute(fn, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes));
         int occ = 0;

@@ -209,3 +209,102 @@ def config_c5(n_inst: int = 96, seed: int = 5, sizes=C5_SIZES):
         p.meta.update(rho=rho, penal=3.0, E0=1.0, Emin=1e-9)
         out.append(p)
     return out
+
+
+# L-shaped domain [0,2]^2 minus (1,2]x(1,2]: model vertices counter-clockwise
+# and the six model segments between them.
+L_SHAPE = np.array([[0.0, 0.0], [2.0, 0.0], [2.0, 1.0], [1.0, 1.0], [1.0, 2.0], [0.0, 2.0]])
+
+
+def _zorder(xy: np.ndarray, bits: int = 16) -> np.ndarray:
+    """Morton (Z-order) keys of points in [0,2]^2 on a 2^bits grid."""
+    q = np.minimum((xy / 2.0 * (1 << bits)).astype(np.uint64), (1 << bits) - 1)
+
+    def spread(v):
+        v = v & np.uint64(0xFFFF)
+        v = (v | (v << np.uint64(8))) & np.uint64(0x00FF00FF)
+        v = (v | (v << np.uint64(4))) & np.uint64(0x0F0F0F0F)
+        v = (v | (v << np.uint64(2))) & np.uint64(0x33333333)
+        v = (v | (v << np.uint64(1))) & np.uint64(0x55555555)
+        return v
+    return spread(q[:, 0]) | (spread(q[:, 1]) << np.uint64(1))
+
+
+def t3_lshape(n_points: int, seed: int = 3, E: float = 1.0, nu: float = 0.25,
+              traction: float = 1.0, name: str = "") -> Problem:
+    """T3 mesh of the L-shaped domain from n_points seeded uniform interior
+    points: Delaunay triangulation of those points plus boundary points at
+    the mean interior spacing, triangles of the notch removed, every
+    boundary edge checked to be a mesh edge (boundary recovery).  Nodes are
+    numbered along a Z-order curve, as a mesher that keeps neighbours close
+    in memory would.  Bottom edge clamped; a +x traction of total `traction`
+    on the segment x = 1, y in [1, 2] (nbots spreads a constant segment load
+    as a total force, set_bconditions.c:133-168)."""
+    from scipy.spatial import Delaunay
+    rng = np.random.Generator(np.random.PCG64(seed))
+    h = np.sqrt(3.0 / n_points)                       # mean spacing (area 3)
+    pts = np.empty((0, 2))
+    while pts.shape[0] < n_points:
+        c = rng.uniform(0.0, 2.0, size=(int(1.4 * (n_points - pts.shape[0])) + 16, 2))
+        keep = ~((c[:, 0] > 1.0) & (c[:, 1] > 1.0))
+        pts = np.concatenate([pts, c[keep]])
+    pts = pts[:n_points]
+    # drop interior points closer than h/2 to the boundary (no slivers there)
+    x, y = pts[:, 0], pts[:, 1]
+    d = np.minimum.reduce([x, y, 2.0 - x, 2.0 - y,
+                           np.where(y > 1.0, np.abs(x - 1.0), np.inf),
+                           np.where(x > 1.0, np.abs(y - 1.0), np.inf)])
+    pts = pts[d > 0.5 * h]
+    # boundary points, segment by segment (each segment's nodes in order)
+    seg_xy = []
+    for s in range(6):
+        a, b = L_SHAPE[s], L_SHAPE[(s + 1) % 6]
+        m = max(1, int(np.ceil(np.linalg.norm(b - a) / h)))
+        t = np.arange(m) / m                          # start vertex, no end vertex
+        seg_xy.append(a[None, :] + t[:, None] * (b - a)[None, :])
+    bnd = np.concatenate(seg_xy)
+    nb = bnd.shape[0]
+    allp = np.concatenate([bnd, pts])
+    order = np.argsort(_zorder(allp), kind="stable")
+    rank = np.empty_like(order)
+    rank[order] = np.arange(order.size)
+    nod = allp[order].astype(np.float64)
+    tri = Delaunay(nod, qhull_options="Qbb Qc Qz Q12").simplices.astype(np.int64)
+    cen = nod[tri].mean(axis=1)
+    tri = tri[~((cen[:, 0] > 1.0) & (cen[:, 1] > 1.0))]
+    # counter-clockwise
+    p0, p1, p2 = nod[tri[:, 0]], nod[tri[:, 1]], nod[tri[:, 2]]
+    area2 = (p1[:, 0] - p0[:, 0]) * (p2[:, 1] - p0[:, 1]) - (p1[:, 1] - p0[:, 1]) * (p2[:, 0] - p0[:, 0])
+    if np.any(area2 == 0.0):
+        raise ValueError("degenerate triangle")
+    flip = area2 < 0
+    tri[flip] = tri[flip][:, [0, 2, 1]]
+    # unique edges
+    e = np.concatenate([tri[:, [0, 1]], tri[:, [1, 2]], tri[:, [2, 0]]])
+    e.sort(axis=1)
+    key = e[:, 0] * nod.shape[0] + e[:, 1]
+    ukey = np.unique(key)
+    edges = np.stack([ukey // nod.shape[0], ukey % nod.shape[0]], axis=1)
+    # model vertices and segments as node sequences; check boundary recovery
+    starts = np.cumsum([0] + [s.shape[0] for s in seg_xy])
+    vtx = rank[starts[:6]].astype(np.uint32)
+    sgm = []
+    for s in range(6):
+        ids = list(range(starts[s], starts[s + 1])) + [starts[(s + 1) % 6]]
+        seq = rank[np.array(ids)].astype(np.uint32)
+        a, b = np.minimum(seq[:-1], seq[1:]), np.maximum(seq[:-1], seq[1:])
+        if not np.all(np.isin(a.astype(np.int64) * nod.shape[0] + b, ukey)):
+            raise ValueError(f"boundary segment {s} not recovered by the triangulation")
+        sgm.append(seq)
+    bcs = [BC(NEUMANN, ON_SEGMENT, 3, (1, 0), (traction, 0.0)),
+           BC(DIRICHLET, ON_SEGMENT, 0, (1, 1), (0.0, 0.0))]
+    Ev = np.full(tri.shape[0], float(E))
+    return Problem(name or f"t3_lshape_{n_points}", "t3", nod, tri.astype(np.uint32),
+                   edges.astype(np.uint32), vtx, sgm, bcs, Ev, nu=nu, thickness=1.0,
+                   meta=dict(n_points=n_points, seed=seed, n_boundary=nb))
+
+
+def config_c3(seed: int = 3, n_points: int = 2_000_000) -> Problem:
+    """T3 L-shape from 2M seeded uniform points (about 4M DOF), E=1, nu=0.25,
+    bottom edge clamped, unit +x traction on x=1, y in [1,2]."""
+    return t3_lshape(n_points, seed=seed, name=f"c3_t3_lshape_{n_points}")
