@@ -105,21 +105,28 @@ __device__ __forceinline__ uint32_t ld_hint(const uint32_t* a, uint64_t pol) {
 // exactly 2^31 once all have arrived, so each block waits (acquire loads)
 // for bit 31 to differ from the value its own atomic returned.  No reset is
 // needed between barriers.  Requires co-residency (cooperative launch).
-// The wait is bounded (kSpinLimitNs, checked every 64 polls).  Returns
-// nonzero when the caller must stop (timeout here or an error recorded by
-// another block).
-__device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, unsigned rank,
-                                            int* status) {
-    __shared__ int s_stop;
+// Split in two so that a block can do work that needs no other block's
+// data between its arrival and its wait.  The wait is bounded
+// (kSpinLimitNs, checked every 64 polls).  barrier_wait returns nonzero when
+// the caller must stop (timeout here or an error recorded by another block).
+__device__ __forceinline__ unsigned barrier_arrive(unsigned* bar, unsigned nblocks,
+                                                   unsigned rank) {
     __syncthreads();
+    unsigned old = 0;
     if (threadIdx.x == 0) {
-        int stop = 0;
         const unsigned add = rank == 0 ? 0x80000000u - (nblocks - 1) : 1u;
-        unsigned old;
         asm volatile("atom.add.release.gpu.global.u32 %0, [%1], %2;"
                      : "=r"(old)
                      : "l"(bar), "r"(add)
                      : "memory");
+    }
+    return old;  // meaningful in thread 0
+}
+
+__device__ __forceinline__ int barrier_wait(unsigned* bar, unsigned old, int* status) {
+    __shared__ int s_stop;
+    if (threadIdx.x == 0) {
+        int stop = 0;
         uint64_t t0 = 0;
         for (unsigned it = 0;; it++) {
             if ((ld_acquire(bar) ^ old) & 0x80000000u) break;
@@ -139,6 +146,12 @@ __device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, uns
     }
     __syncthreads();
     return s_stop;
+}
+
+__device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, unsigned rank,
+                                            int* status) {
+    const unsigned old = barrier_arrive(bar, nblocks, rank);
+    return barrier_wait(bar, old, status);
 }
 
 // Block-wide sum of NV values per thread, fixed tree order.  Result valid in

@@ -78,14 +78,12 @@ constexpr int kUnroll = NBG_MIXED_UNROLL;
 #ifndef NBG_L2_KEEP
 #define NBG_L2_KEEP 50  // percent of L2 for the matrix part kept between iterations
 #endif
-#ifndef NBG_MIXED_PREFETCH
-#define NBG_MIXED_PREFETCH 0  // L2 bulk prefetch of upcoming slices in the SpMV
-#endif
 
 namespace {
 
 // Low parts of p and of A p: bfloat16 (FP32 hi + 8 bits) or FP32 (hi + lo
 // about 48 bits), chosen separately (NBG_MIXED_PLO32, NBG_MIXED_WLO32).
+#if !NBG_MIXED_PLO32 || !NBG_MIXED_WLO32
 struct LoBF {
     using one = __nv_bfloat16;
     using two = __nv_bfloat162;
@@ -97,6 +95,7 @@ struct LoBF {
         return __bfloat162float(__float2bfloat16_rn(x));
     }
 };
+#endif
 struct LoF32 {
     using one = float;
     using two = float2;
@@ -192,24 +191,6 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     }
     y0 = t[0];
     y1 = t[1];
-}
-
-// Bring slice s's matrix stream (FP32 values, remainders, columns: one
-// contiguous range per array) into L2 with three bulk prefetches issued by
-// one lane.  The copy engine fetches ahead while the warp works on earlier
-// slices, so the SpMV's loads find L2 instead of waiting on HBM, without
-// holding registers.  Sizes are multiples of 128 B and starts 128 B-aligned.
-__device__ __forceinline__ void l2_prefetch(const void* p, uint32_t bytes) {
-    asm volatile("cp.async.bulk.prefetch.L2.global [%0], %1;" ::"l"(p), "r"(bytes) : "memory");
-}
-
-__device__ __forceinline__ void prefetch_slice(const nbg_bsr_t& A, uint32_t s) {
-    const uint32_t k0 = A.slice_off[s], n = A.slice_off[s + 1] - k0;
-    if (n == 0) return;
-    const size_t e0 = (size_t)k0 * 32;
-    l2_prefetch(A.b32 + 4 * e0, n * 32 * 16);
-    l2_prefetch(A.blo + 4 * e0, n * 32 * 8);
-    l2_prefetch(A.bcol + e0, n * 32 * 4);
 }
 
 // Own-row vectors of this block, indexed by local node row
@@ -362,15 +343,8 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
         {   // L1: w = A p, p.w (two lanes per node row)
             FFAcc pw{0.f, 0.f};
             const uint32_t par = lane >> 4, nh = 2 * (s1 - s0);
-            // warp w takes half slices w, w + nw, ...: the slices of the even
-            // warps' first two rounds are prefetched now, each later round's
-            // two rounds ahead
-            if (NBG_MIXED_PREFETCH && lane == 0 && !(warp & 1))
-                for (uint32_t h = warp; h < nh && h < warp + 2 * nw; h += nw)
-                    prefetch_slice(a.A, s0 + (h >> 1));
+            // warp w takes half slices w, w + nw, ...
             for (uint32_t h = warp; h < nh; h += nw) {
-                if (NBG_MIXED_PREFETCH && lane == 0 && !(warp & 1) && h + 2 * nw < nh)
-                    prefetch_slice(a.A, s0 + ((h + 2 * nw) >> 1));
                 const uint32_t s = s0 + (h >> 1), r = ((h & 1) << 4) | (lane & 15);
                 const uint32_t i = s * 32 + r, li = i - s0 * 32;
                 // a slice's rows past Nn are padding: skip them whole (both lanes)
