@@ -514,7 +514,30 @@ def run_gpu(args):
     t_csr = spmv_time(lambda: lib.nbg_spmv_csr_f64(N, rp, ci, K, x64.data_ptr(), y64.data_ptr(), sp))
     t_b64 = spmv_time(lambda: lib.nbg_spmv_bsr_f64(C.byref(A), x64.data_ptr(), y64.data_ptr(), sp))
     t_b32 = spmv_time(lambda: lib.nbg_spmv_bsr_f32(C.byref(A), x32.data_ptr(), y32.data_ptr(), sp))
+    # the mixed solver's operator alone: cold (L2 flushed before each launch)
+    # and repeated back to back without a flush, as inside a solve, where
+    # the evict_last share of the matrix stays in L2 between launches
+    ph32 = x64.float()
+    pl32 = (x64 - ph32.double()).float()
+    wh32 = torch.empty_like(ph32)
+    wl32 = torch.empty_like(ph32)
+
+    def mixed_op():
+        lib.nbg_spmv_bsr_mixed(C.byref(A), ph32.data_ptr(), pl32.data_ptr(), wh32.data_ptr(),
+                               wl32.data_ptr(), sp)
+    t_mix_cold = spmv_time(mixed_op)
+    for _ in range(5):
+        mixed_op()
+    e0 = torch.cuda.Event(enable_timing=True)
+    e1 = torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(50):
+        mixed_op()
+    e1.record(stream)
+    e1.synchronize()
+    t_mix_warm = e0.elapsed_time(e1) / 1e3 / 50
     hbm, peak_kind = peaks()
+    B_mix = 28 * nblk + 4 * (A.n_slices + 1) + 16 * N
     B_csr = 12 * nnz + 4 * (N + 1) + 8 * N + 8 * N
     B_b64 = 36 * nblk + 4 * (A.n_slices + 1) + 16 * N
     B_b32 = 20 * nblk + 4 * (A.n_slices + 1) + 8 * N
@@ -524,6 +547,12 @@ def run_gpu(args):
                            "frac": B_b64 / t_b64 / 1e9 / hbm, "bytes": B_b64},
             "fp32_block": {"us": t_b32 * 1e6, "gbs": B_b32 / t_b32 / 1e9,
                            "frac": B_b32 / t_b32 / 1e9 / hbm, "bytes": B_b32},
+            "mixed_operator_cold": {"us": t_mix_cold * 1e6, "gbs": B_mix / t_mix_cold / 1e9,
+                                    "frac": B_mix / t_mix_cold / 1e9 / hbm, "bytes": B_mix},
+            "mixed_operator_repeated": {"us": t_mix_warm * 1e6, "gbs": B_mix / t_mix_warm / 1e9,
+                                        "frac": B_mix / t_mix_warm / 1e9 / hbm,
+                                        "bytes": B_mix,
+                                        "l2": "50 launches back to back, no flush"},
             "peak_gbs": hbm, "peak_kind": peak_kind, "l2": "flushed before each launch"}
 
     # ---- roofline of the mixed solver kernel: algorithmic bytes per iteration,

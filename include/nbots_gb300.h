@@ -213,6 +213,13 @@ typedef struct {
     double bnorm;
 } nbg_mixed_result_t;
 
+/* The mixed solver's SpMV operator on its own: w = A p with A = b32 + blo and
+ * p = ph + pl (FP32 pairs), products and sums error-free, result as
+ * wh + wl (FP32 pairs); the first share of the matrix stream is loaded with
+ * an L2 evict_last policy, as inside the solver. */
+int nbg_spmv_bsr_mixed(const nbg_bsr_t *A, const float *ph, const float *pl, float *wh,
+                       float *wl, void *stream);
+
 size_t nbg_cg_mixed_workspace_bytes(uint32_t N);
 int nbg_cg_mixed(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_iter,
                  double tol, double delta, unsigned flags, nbg_mixed_result_t *result,

@@ -96,6 +96,7 @@ SIGS = {
     "nbg_cg_bsr_workspace_bytes": ([u32], sz),
     "nbg_cg_bsr_f64": ([C.POINTER(Bsr), vp, vp, u32, f64, C.c_uint, C.POINTER(CgResult), vp,
                         sz, vp], i32),
+    "nbg_spmv_bsr_mixed": ([C.POINTER(Bsr), vp, vp, vp, vp, vp], i32),
     "nbg_cg_mixed_workspace_bytes": ([u32], sz),
     "nbg_cg_mixed": ([C.POINTER(Bsr), vp, vp, u32, f64, f64, C.c_uint,
                       C.POINTER(MixedResult), vp, sz, vp], i32),

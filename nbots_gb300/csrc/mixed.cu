@@ -557,7 +557,52 @@ size_t mixed_bytes(uint32_t N) {
     return 5 * f + 2 * h + align256(kMaxBlocks * 6 * 8) + 3 * 256;
 }
 
+// The mixed solver's SpMV operator as its own launch: w = A p with the split
+// matrix and float-float p, two lanes per node row, the solver's L2 policy
+// (the first keep_pm / 1000 of each block's slices evict_last).  One block per
+// SM, slices split evenly, as in the solver.
+__global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
+    k_spmv_mixed(MixArgs a, float2* __restrict__ wh, LoW::two* __restrict__ wl) {
+    uint32_t s0, s1;
+    slice_range(a.A.n_slices, s0, s1);
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nw = kMixThreads / 32, par = lane >> 4, nh = 2 * (s1 - s0);
+    for (uint32_t h = warp; h < nh; h += nw) {
+        const uint32_t s = s0 + (h >> 1), r = ((h & 1) << 4) | (lane & 15);
+        const uint32_t i = s * 32 + r;
+        if (s * 32 + ((h & 1) << 4) >= a.A.Nn) continue;
+        FF y0, y1;
+        const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
+        spmv_half_split(a, s, r, par, i < a.A.Nn, pol, y0, y1);
+        if (par || i >= a.A.Nn) continue;
+        wh[i] = make_float2(y0.hi, y1.hi);
+        wl[i] = LoW::pack(LoW::round(y0.lo), LoW::round(y1.lo));
+    }
+}
+
 }  // namespace
+
+extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const float* pl,
+                                  float* wh, float* wl, void* stream) {
+    if (!A || !A->b32 || !A->blo || !ph || !pl || !wh || !wl) return NBG_ERR_ARG;
+    if (sizeof(LoP::one) != 4 || sizeof(LoW::one) != 4) return NBG_ERR_ARG;  // FP32 low parts
+    if (A->Nn == 0) return NBG_OK;
+    MixArgs a;
+    memset(&a, 0, sizeof(a));
+    a.A = *A;
+    a.ph = const_cast<float*>(ph);
+    a.pl = reinterpret_cast<LoP::one*>(const_cast<float*>(pl));
+    a.keep_pm = keep_permille(*A);
+    unsigned G = 0;
+    const int rc = coop_grid((const void*)k_spmv_mixed, A->n_slices, &G, kMixThreads);
+    if (rc != NBG_OK) return rc;
+    k_spmv_mixed<<<G, kMixThreads, 0, (cudaStream_t)stream>>>(
+        a, reinterpret_cast<float2*>(wh), reinterpret_cast<LoW::two*>(wl));
+    NBG_CHECK(cudaGetLastError());
+    return NBG_OK;
+}
+
+
 
 extern "C" size_t nbg_cg_mixed_workspace_bytes(uint32_t N) { return mixed_bytes(N); }
 
