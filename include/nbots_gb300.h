@@ -178,15 +178,6 @@ int nbg_bsr_fill(const nbg_bsr_t *A, const uint32_t *row_ptr, const uint32_t *co
                  const double *val, void *stream);
 int nbg_spmv_bsr_f64(const nbg_bsr_t *A, const double *x, double *y, void *stream);
 int nbg_spmv_bsr_f32(const nbg_bsr_t *A, const float *x, float *y, void *stream);
-/* Streamed SpMVs: each warp moves its slices of the matrix into shared
- * memory with cp.async.bulk (double-buffered, mbarrier completion).
- * _split: y = (b32 + blo)(xh + xl) with error-free FP32 arithmetic, y as
- * yh (FP32) + yl (bfloat16 bits); the operator of nbg_cg_mixed.
- * status: one device int, NBG_ERR_TIMEOUT if a copy never completed. */
-int nbg_spmv_bsr_split(const nbg_bsr_t *A, const float *xh, const uint16_t *xl, float *yh,
-                       uint16_t *yl, int *status, void *stream);
-int nbg_spmv_bsr_f64_stream(const nbg_bsr_t *A, const double *x, double *y, int *status,
-                            void *stream);
 
 /* Fast persistent FP64 Jacobi-PCG on the block layout: FMA arithmetic,
  * reciprocal diagonal, stop on the current ||g|| (not nbots' lagged one);

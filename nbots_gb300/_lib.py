@@ -91,8 +91,6 @@ SIGS = {
     "nbg_bsr_fill": ([C.POINTER(Bsr), vp, vp, vp, vp], i32),
     "nbg_spmv_bsr_f64": ([C.POINTER(Bsr), vp, vp, vp], i32),
     "nbg_spmv_bsr_f32": ([C.POINTER(Bsr), vp, vp, vp], i32),
-    "nbg_spmv_bsr_split": ([C.POINTER(Bsr), vp, vp, vp, vp, vp, vp], i32),
-    "nbg_spmv_bsr_f64_stream": ([C.POINTER(Bsr), vp, vp, vp, vp], i32),
     "nbg_cg_bsr_workspace_bytes": ([u32], sz),
     "nbg_cg_bsr_f64": ([C.POINTER(Bsr), vp, vp, u32, f64, C.c_uint, C.POINTER(CgResult), vp,
                         sz, vp], i32),

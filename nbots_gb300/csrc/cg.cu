@@ -1,22 +1,24 @@
 // Persistent FP64 (Jacobi-preconditioned) CG: one cooperative launch runs
 // the whole solve with device-side convergence checks.
 //
-// Iteration (nbots' cg_precond_jacobi.c:45-76):
+// Iteration (nbots' cg_precond_jacobi.c:45-76), three grid barriers:
 //   L1: w = A p; dot_pw, dot_gg (old g), dot_gq
 //   L2: alpha = gq/pw; x += alpha p; g += alpha w; q = g / Aii; dot_gkqk
 //   L3: beta = gkqk/gq; p = -q + beta p
-// Here L3 is folded into the next L1: every block forms p_k = -q + beta
-// p_{k-1} for its own rows (written to the other half of a double buffer)
-// and recomputes the same expression, bit for bit, for the columns it
-// gathers.  That leaves two grid barriers per iteration.  Per-row work
-// repeats nbots' arithmetic (rounded products, left-to-right row sums,
-// division by the diagonal); the dot products are block-tree plus a fixed
-// block order, identical from run to run.
+// Per-row work repeats nbots' arithmetic (rounded products, left-to-right
+// row sums, division by the diagonal).  GB300 issues FP64 at about two
+// operations per SM per clock, so the SpMV's two FP64 operations per nonzero
+// bound the iteration: folding L3 into the next SpMV (recomputing -q + beta p
+// for every gathered column) saves a barrier but costs five per nonzero; on
+// the 1M-dof cantilever the folded form took 1.58 s for 7,017 iterations,
+// this one 1.11 s.  The scalar recurrences run in thread 0;
+// the dot products are summed by warp 0 in a fixed order, identical from run
+// to run.
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
 
-#include "common.cuh"
+#include "persist.cuh"
 
 using namespace nbg;
 
@@ -55,38 +57,26 @@ struct CgArgs {
     unsigned flags;
 };
 
-// Sum of NV partials per block over all blocks in block order; every block
-// gets the same bits.
-template <int NV>
-__device__ __forceinline__ void grid_reduce(const double* part, double* out, double* sh) {
-    const unsigned G = gridDim.x;
-    if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
-#pragma unroll
-        for (int k = 0; k < NV; k++) {
-            double s = 0.0;
-            for (unsigned b = lane; b < G; b += 32) s = add(s, part[b * NV + k]);
-#pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s = add(s, __shfl_down_sync(0xffffffffu, s, o));
-            if (lane == 0) sh[k] = s;
-        }
-    }
-    __syncthreads();
-#pragma unroll
-    for (int k = 0; k < NV; k++) out[k] = sh[k];
-    __syncthreads();
-}
-
 template <bool JAC>
 __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
-    __shared__ double red[3 * 32];
-    __shared__ double bc[4];
+    __shared__ double buf[3 * kThreads];
+    __shared__ double s_coef;  // alpha, then beta
+    __shared__ int s_stop;
+    __shared__ struct {
+        double gg, bb, gq, tol2;
+        uint32_t k;
+    } sc;  // scalar state, thread 0 only
     const unsigned G = gridDim.x;
     const uint32_t per = (a.N + G - 1) / G;
     const uint32_t r0 = min(blockIdx.x * per, a.N), r1 = min(r0 + per, a.N);
     const uint32_t* __restrict__ rp = a.rp;
     const uint32_t* __restrict__ ci = a.ci;
     const double* __restrict__ val = a.val;
+    double* __restrict__ p = a.P0;
+    if (threadIdx.x == 0) {
+        sc.gg = sc.bb = sc.gq = sc.tol2 = 0.0;
+        sc.k = 0;
+    }
 
     // init (cg_precond_jacobi.c:33-43)
     {
@@ -103,100 +93,101 @@ __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
             a.g[r] = gi;
             a.Aii[r] = d;
             a.q[r] = qi;
-            a.P0[r] = -qi;
+            p[r] = -qi;
             v[0] = add(v[0], mul(gi, gi));
             v[1] = add(v[1], mul(a.b[r], a.b[r]));
         }
-        block_sum<2>(v, red);
+        double t[2];
+        block_sum_f64<2>(v, buf, t);
         if (threadIdx.x == 0) {
-            a.partC[blockIdx.x * 2] = v[0];
-            a.partC[blockIdx.x * 2 + 1] = v[1];
+            a.partC[blockIdx.x * 2] = t[0];
+            a.partC[blockIdx.x * 2 + 1] = t[1];
         }
     }
-    uint32_t k = 0;
-    double dot_gg = 0.0, bb = 0.0;
     if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
     {
         double t[2];
-        grid_reduce<2>(a.partC, t, bc);
-        dot_gg = t[0];
-        bb = t[1];
+        group_reduce0<2>(a.partC, G, t);
+        if (threadIdx.x == 0) {
+            sc.gg = t[0];
+            sc.bb = t[1];
+            const double tolb = (a.flags & NBG_CG_RELATIVE) ? a.tol * sqrt(sc.bb) : a.tol;
+            sc.tol2 = tolb * tolb;
+            s_stop = !(sc.gg > sc.tol2) || a.max_iter == 0;
+        }
+        __syncthreads();
     }
-    {
-        const double tolb = (a.flags & NBG_CG_RELATIVE) ? a.tol * sqrt(bb) : a.tol;
-        const double tol2 = tolb * tolb;
-        double beta = 0.0;
-        while (dot_gg > tol2 && k < a.max_iter) {
-            double* __restrict__ pk = (k & 1) ? a.P1 : a.P0;
-            const double* __restrict__ pprev = (k & 1) ? a.P0 : a.P1;
-            const double* __restrict__ q = a.q;
-            // L1 with the p update of the previous L3 folded in
+    while (!s_stop) {
+        {   // L1: w = A p; p.w, g.g (the lagged norm nbots tests), g.q
             double v3[3] = {0.0, 0.0, 0.0};
             for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
-                double pr, s = 0.0;
-                if (k == 0) {
-                    pr = pk[r];
-                    for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++)
-                        s = add(s, mul(val[kk], pk[ci[kk]]));
-                } else {
-                    pr = add(-q[r], mul(beta, pprev[r]));
-                    pk[r] = pr;
-                    for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++) {
-                        const uint32_t c = ci[kk];
-                        s = add(s, mul(val[kk], add(-q[c], mul(beta, pprev[c]))));
-                    }
-                }
+                double s = 0.0;
+                for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++) s = add(s, mul(val[kk], p[ci[kk]]));
                 a.w[r] = s;
-                const double gi = a.g[r], qi = q[r];
-                v3[0] = add(v3[0], mul(pr, s));
+                const double gi = a.g[r], qi = a.q[r];
+                v3[0] = add(v3[0], mul(p[r], s));
                 v3[1] = add(v3[1], mul(gi, gi));
                 v3[2] = add(v3[2], mul(gi, qi));
             }
-            block_sum<3>(v3, red);
-            if (threadIdx.x == 0) {
-                a.partA[blockIdx.x * 3] = v3[0];
-                a.partA[blockIdx.x * 3 + 1] = v3[1];
-                a.partA[blockIdx.x * 3 + 2] = v3[2];
-            }
-            if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
+            double t[3];
+            block_sum_f64<3>(v3, buf, t);
+            if (threadIdx.x == 0)
+                for (int j = 0; j < 3; j++) a.partA[blockIdx.x * 3 + j] = t[j];
+        }
+        if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
+        {
             double t3[3];
-            grid_reduce<3>(a.partA, t3, bc);
-            const double dot_pw = t3[0], dot_gq = t3[2];
-            dot_gg = t3[1];
-            const double alpha = dvd(dot_gq, dot_pw);
-            // L2
+            group_reduce0<3>(a.partA, G, t3);
+            if (threadIdx.x == 0) {
+                sc.gg = t3[1];
+                sc.gq = t3[2];
+                s_coef = dvd(t3[2], t3[0]);  // alpha = gq / pw
+            }
+            __syncthreads();
+        }
+        {   // L2: x += alpha p; g += alpha w; q = g / Aii; g.q
+            const double alpha = s_coef;
             double v1[1] = {0.0};
             for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
-                a.x[r] = add(a.x[r], mul(alpha, pk[r]));
+                a.x[r] = add(a.x[r], mul(alpha, p[r]));
                 const double gi = add(a.g[r], mul(alpha, a.w[r]));
                 a.g[r] = gi;
                 const double qi = JAC ? dvd(gi, a.Aii[r]) : gi;
                 a.q[r] = qi;
                 v1[0] = add(v1[0], mul(gi, qi));
             }
-            block_sum<1>(v1, red);
-            if (threadIdx.x == 0) a.partB[blockIdx.x] = v1[0];
-            if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
-            double t1[1];
-            grid_reduce<1>(a.partB, t1, bc);
-            beta = dvd(t1[0], dot_gq);
-            k++;
+            double t[1];
+            block_sum_f64<1>(v1, buf, t);
+            if (threadIdx.x == 0) a.partB[blockIdx.x] = t[0];
         }
+        if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
+        {
+            double t1[1];
+            group_reduce0<1>(a.partB, G, t1);
+            if (threadIdx.x == 0) {
+                s_coef = dvd(t1[0], sc.gq);  // beta
+                sc.k++;
+                s_stop = !(sc.gg > sc.tol2) || sc.k >= a.max_iter;
+            }
+            __syncthreads();
+        }
+        if (s_stop) break;
+        {   // L3: p = -q + beta p
+            const double beta = s_coef;
+            for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads)
+                p[r] = add(-a.q[r], mul(beta, p[r]));
+        }
+        if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
     }
 done:
     if (blockIdx.x == 0 && threadIdx.x == 0) {
-        const double tolb = (a.flags & NBG_CG_RELATIVE) ? a.tol * sqrt(bb) : a.tol;
-        a.res->niter = k;
-        a.res->dot_gg = dot_gg;
-        a.res->bb = bb;
+        a.res->niter = sc.k;
+        a.res->dot_gg = sc.gg;
+        a.res->bb = sc.bb;
         int st = ld_volatile(a.status);
-        a.res->status = st != 0 ? st : (dot_gg > tolb * tolb ? NBG_NOT_CONVERGED : NBG_OK);
+        a.res->status = st != 0 ? st : (sc.gg > sc.tol2 ? NBG_NOT_CONVERGED : NBG_OK);
     }
 }
-
-inline size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
-
-constexpr unsigned kMaxBlocks = 4096;
 
 struct Layout {
     size_t g, q, P0, P1, w, Aii, partA, partB, partC, bar, status, res, total;

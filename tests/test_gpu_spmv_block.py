@@ -2,11 +2,10 @@
 same matrix (nbots' K after boundary conditions) and vector.
 
 Bars, relative to max|y|: FP64 block SpMV 1e-14 (FMA order differs from
-nbots'); FP32 values and vector 1e-6; the split operators (FP32 + 16-bit
-remainder matrix, about 40 bits, times a float-float vector, error-free
-sums) 1e-10; the streamed variants equal their direct counterparts' bars.
-Every entry point also leaves rows past the last node untouched and handles
-a system whose node count is not a multiple of the 32-row slice."""
+nbots'); FP32 values and vector 1e-6; the mixed solver's operator (FP32 +
+16-bit remainder matrix, about 40 bits, times a float-float vector,
+error-free sums) 1e-10.  The cases include systems whose node count is not a
+multiple of the 32-row slice."""
 import ctypes as C
 
 import numpy as np
@@ -55,19 +54,12 @@ def test_fp64_and_fp32_block_spmv(L, name):
     dx32, dy32 = DeviceArray(x32), DeviceArray(shape=(s.N,), dtype=np.float32)
     assert lib.nbg_spmv_bsr_f32(C.byref(A), dx32.ptr, dy32.ptr, None) == 0
     assert err(dy32.numpy().astype(np.float64), y_ref) < 1e-6
-    # streamed FP64 variant
-    st = DeviceArray(np.zeros(1, np.int32))
-    dy.upload(np.zeros(s.N))
-    assert lib.nbg_spmv_bsr_f64_stream(C.byref(A), dx.ptr, dy.ptr, st.ptr, None) == 0
-    assert st.numpy()[0] == 0
-    assert err(dy.numpy(), y_ref) < 1e-14
     s.close()
 
 
 @pytest.mark.parametrize("name", CASES)
-def test_split_operators(L, name):
-    """nbg_spmv_bsr_mixed (the mixed solver's operator) with FP32 low parts
-    and nbg_spmv_bsr_split (streamed, bfloat16 low parts of x and y)."""
+def test_mixed_operator(L, name):
+    """nbg_spmv_bsr_mixed: the mixed solver's operator with FP32 low parts."""
     from nbots_gb300.device import DeviceArray
     lib = L.lib()
     s, A, x, y_ref = setup(L, name, seed=1)
@@ -83,19 +75,4 @@ def test_split_operators(L, name):
     assert lib.nbg_spmv_bsr_mixed(C.byref(A), dxh.ptr, dxl.ptr, dwh.ptr, dwl.ptr, None) == 0
     y = dwh.numpy().astype(np.float64) + dwl.numpy().astype(np.float64)
     assert err(y, y_ff) < 1e-10
-    # streamed split operator: x low part and y low part as bfloat16 bits
-    xl16 = (xl.view(np.uint32) >> 16).astype(np.uint16)   # truncation toward zero
-    xl_b = (xl16.astype(np.uint32) << 16).view(np.float32).astype(np.float64)
-    y_b = O.spmv(d["row_ptr"], d["col_idx"], d["K_bc"], xh.astype(np.float64) + xl_b)
-    dxl16 = DeviceArray(xl16)
-    dyh = DeviceArray(shape=(s.N,), dtype=np.float32)
-    dyl = DeviceArray(shape=(s.N,), dtype=np.uint16)
-    st = DeviceArray(np.zeros(1, np.int32))
-    assert lib.nbg_spmv_bsr_split(C.byref(A), dxh.ptr, dxl16.ptr, dyh.ptr, dyl.ptr, st.ptr,
-                                  None) == 0
-    assert st.numpy()[0] == 0
-    yl = (dyl.numpy().astype(np.uint32) << 16).view(np.float32).astype(np.float64)
-    y2 = dyh.numpy().astype(np.float64) + yl
-    # the bfloat16 low part of y keeps about 32 bits of the result
-    assert err(y2, y_b) < 1e-8
     s.close()
