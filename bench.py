@@ -387,17 +387,16 @@ def run_c3(args):
 
 def run_gpu(args):
     import torch
-    import torch.distributed as dist
     from nbots_gb300 import _lib as L
+    from nbots_gb300 import replicas as R
     from nbots_gb300 import workloads as W
     from nbots_gb300.fem import FemSystem
 
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    if world > 1:
-        dist.init_process_group("nccl")
+    # replicas only: every rank solves the same system on its own GPU, with
+    # no collective on the data path (barrier and max of times only)
+    rank, world, local = R.world()
     torch.cuda.set_device(local)
+    R.init("nccl")
     lib = L.lib()
     dev = torch.device("cuda", local)
     stream = torch.cuda.current_stream(dev)
@@ -405,8 +404,7 @@ def run_gpu(args):
 
     def barrier():
         torch.cuda.synchronize()
-        if world > 1:
-            dist.barrier()
+        R.barrier()
 
     # ---- problem: assemble and apply BCs on the device (timed once)
     p = W.config_c2()
@@ -620,10 +618,7 @@ def run_gpu(args):
         lib.nbg_host_free(ptr)
 
     # ---- max over ranks
-    vals = torch.tensor([t_med, e2e_v], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(vals, op=dist.ReduceOp.MAX)
-    t_all, e2e_all = float(vals[0]), float(vals[1])
+    t_all, e2e_all = R.max_over_ranks([t_med, e2e_v], device=dev)
 
     c4 = None if args.no_c4 else bench_c4(lib, L, W)
     c5 = None if args.no_c5 else bench_c5(args, lib, L, W, sp, dev, stream, flush)
@@ -636,7 +631,8 @@ def run_gpu(args):
             "metric": METRIC, "value": t_all, "unit": "s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 inner (FP32+bf16 split operands) / f64 residual", "data": "synthetic",
+            "dtype": "f32 inner (float-float p, A p, x; FP32 + 16-bit remainder matrix) / f64 "
+                     "residual", "data": "synthetic",
             "config": {"workload": WORKLOAD, "dof": N, "nnz": nnz, "tol": TOL,
                        "l2": "flushed (512 MB write) before every timed solve",
                        "replicas": world},
@@ -674,8 +670,7 @@ def run_gpu(args):
             "clocks": clk.summary(),
         }
         print(json.dumps(line))
-    if world > 1:
-        dist.destroy_process_group()
+    R.finalize()
     s.close()
     return 0
 
