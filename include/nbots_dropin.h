@@ -131,6 +131,11 @@ void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t 
 				       double *strain, const bool *elements_enabled,
 				       double *stress);
 
+/* pipeline.h:42-45, pipeline.c:321-340: principal stresses (sx + sy)/2 +-
+ * sqrt((sx - sy)^2/4 + txy^2) per Gauss point, bit-exact. */
+void pipeline_compute_main_stress(double *stress, double *main_stress, uint32_t N_elements,
+				  const nb_fem_elem_t *const elem);
+
 /* Last error of a drop-in call that nbots would have ended with exit(1)
  * (0 if none); cleared by reading. */
 int nbg_dropin_error(void);

@@ -103,6 +103,10 @@ int nbg_strain_f64(uint32_t nen, uint32_t N_elem, const double *nod, const uint3
 int nbg_stress_f64(uint32_t nen, uint32_t N_elem, const double *E, double nu,
                    const uint8_t *enabled, const double *strain, double *stress,
                    void *stream);
+/* Principal stresses (pipeline_compute_main_stress, pipeline.c:321-340):
+ * main_stress[2 N_gp N_elem] from stress[3 N_gp N_elem]; bit-exact. */
+int nbg_main_stress_f64(uint32_t nen, uint32_t N_elem, const double *stress,
+                        double *main_stress, void *stream);
 
 /* ------------------------------------------------------------------ SpMV */
 /* y = A x with nbots' per-row left-to-right sum and no FMA
@@ -348,6 +352,8 @@ int nbg_fem_solve_mixed(nbg_fem_t *f, uint32_t max_iter, double tol, double delt
                         unsigned flags, nbg_mixed_result_t *res);
 int nbg_fem_strain(nbg_fem_t *f);
 int nbg_fem_stress(nbg_fem_t *f);
+/* Principal stresses from the current stress (NBG_FEM_MAIN_STRESS). */
+int nbg_fem_main_stress(nbg_fem_t *f);
 
 /* ------------------------------------------------------------------ SIMP */
 /* SIMP element sensitivities (no counterpart in nbots): with
@@ -385,6 +391,7 @@ int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double n
 #define NBG_FEM_E 7         /* double[N_elem] */
 #define NBG_FEM_NOD 8       /* double[2 N_nod] */
 #define NBG_FEM_CONN 9      /* uint32[nen N_elem] */
+#define NBG_FEM_MAIN_STRESS 10  /* double[2 N_gp N_elem] */
 /* Device pointer of one array, and a copy of it to host memory. */
 void *nbg_fem_device_ptr(nbg_fem_t *f, int what);
 size_t nbg_fem_bytes(const nbg_fem_t *f, int what);

@@ -81,6 +81,8 @@ SIGS = {
     "nbg_dirichlet_f64": ([u32, vp, vp, vp, vp, vp, vp, vp, vp, vp], i32),
     "nbg_strain_f64": ([u32, u32, vp, vp, vp, vp, vp], i32),
     "nbg_stress_f64": ([u32, u32, vp, f64, vp, vp, vp, vp], i32),
+    "nbg_main_stress_f64": ([u32, u32, vp, vp, vp], i32),
+    "nbg_fem_main_stress": ([vp], i32),
     "nbg_spmv_csr_f64": ([u32, vp, vp, vp, vp, vp, vp], i32),
     "nbg_cg_workspace_bytes": ([u32], sz),
     "nbg_cg_f64": ([u32, vp, vp, vp, vp, vp, u32, f64, C.c_uint, C.POINTER(CgResult), vp, sz,
@@ -150,7 +152,7 @@ SIGS = {
 }
 
 (FEM_ROW_PTR, FEM_COL_IDX, FEM_K, FEM_F, FEM_U, FEM_STRAIN, FEM_STRESS, FEM_E, FEM_NOD,
- FEM_CONN) = range(10)
+ FEM_CONN, FEM_MAIN_STRESS) = range(11)
 CG_JACOBI, CG_RELATIVE = 1, 2
 METHOD_NBOTS, METHOD_FP64, METHOD_MIXED = 0, 1, 2
 PATTERN_SAME = 1

@@ -363,9 +363,37 @@ __global__ void k_stress(uint32_t N_elem, int ngp, const double* __restrict__ E,
     }
 }
 
+// Principal stresses per Gauss point (pipeline.c:321-340): the mean of the
+// normal stresses plus and minus the radius of Mohr's circle, nbots'
+// operation order without contraction and a correctly rounded square root.
+__global__ void k_main_stress(uint32_t n, const double* __restrict__ stress,
+                              double* __restrict__ main_stress) {
+    const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const double sx = stress[(size_t)i * 3], sy = stress[(size_t)i * 3 + 1];
+    const double txy = stress[(size_t)i * 3 + 2];
+    const double avg = mul(0.5, add(sx, sy));
+    const double d = sub(sx, sy);
+    const double R = __dsqrt_rn(add(mul(0.25, mul(d, d)), mul(txy, txy)));
+    main_stress[(size_t)i * 2] = add(avg, R);
+    main_stress[(size_t)i * 2 + 1] = sub(avg, R);
+}
+
 inline unsigned nblk(uint64_t n, unsigned t) { return (unsigned)((n + t - 1) / t); }
 
 }  // namespace
+
+extern "C" int nbg_main_stress_f64(uint32_t nen, uint32_t N_elem, const double* stress,
+                                   double* main_stress, void* stream) {
+    if (nen != 3 && nen != 4) return NBG_ERR_ARG;
+    const uint64_t n = (uint64_t)N_elem * (nen == 4 ? 4 : 1);
+    if (n == 0) return NBG_OK;
+    if (n > UINT32_MAX) return NBG_ERR_ARG;
+    k_main_stress<<<nblk(n, 256), 256, 0, (cudaStream_t)stream>>>((uint32_t)n, stress,
+                                                                  main_stress);
+    NBG_CHECK(cudaGetLastError());
+    return NBG_OK;
+}
 
 extern "C" int nbg_element_stiffness_f64(uint32_t nen, uint32_t N_elem, const double* nod,
                                          const uint32_t* conn, const double* E, double nu,

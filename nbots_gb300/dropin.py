@@ -75,6 +75,8 @@ def libs():
         G.nb_fem_compute_2D_Solid_Mechanics.restype = C.c_int
         G.nb_fem_compute_stress_from_strain.argtypes = [u32, vp, vp, C.c_int, vp, vp, vp]
         G.nb_fem_compute_stress_from_strain.restype = None
+        G.pipeline_compute_main_stress.argtypes = [vp, vp, u32, vp]
+        G.pipeline_compute_main_stress.restype = None
         G.nbg_dropin_error.restype = C.c_int
         H.nbh_mesh2D_create.argtypes = [u32, u32, vp, u32, vp, u32, vp, u32, vp, u32, vp, vp]
         H.nbh_mesh2D_create.restype = vp
@@ -185,6 +187,14 @@ class NbotsObjects:
         G.nb_fem_compute_stress_from_strain(p.n_elems, self.elem, self.mat, 0, s.ctypes.data,
                                             None if en is None else en.ctypes.data,
                                             out.ctypes.data)
+        return out
+
+    def main_stress(self, stress):
+        """pipeline_compute_main_stress through the drop-in symbol."""
+        G, _ = libs()
+        s = np.ascontiguousarray(stress, np.float64)
+        out = np.zeros(2 * (s.size // 3))
+        G.pipeline_compute_main_stress(s.ctypes.data, out.ctypes.data, self.p.n_elems, self.elem)
         return out
 
     def close(self):

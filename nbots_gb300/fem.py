@@ -124,6 +124,10 @@ class FemSystem:
         L.check(self.lib.nbg_fem_stress(self.handle), "stress")
         return self.get(L.FEM_STRESS)
 
+    def main_stress(self):
+        L.check(self.lib.nbg_fem_main_stress(self.handle), "main_stress")
+        return self.get(L.FEM_MAIN_STRESS)
+
     _DT = {L.FEM_ROW_PTR: np.uint32, L.FEM_COL_IDX: np.uint32}
 
     def get(self, what):

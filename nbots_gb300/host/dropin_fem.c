@@ -262,3 +262,19 @@ void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t 
 	free(E);
 	free(en);
 }
+
+void pipeline_compute_main_stress(double *stress, double *main_stress, uint32_t N_elements,
+				  const nb_fem_elem_t *const elem)
+{
+	const uint32_t nen = nb_fem_elem_get_N_nodes(elem);
+	const size_t n = (size_t)nb_fem_elem_get_N_gpoints(elem) * N_elements;
+	void *ds = NULL, *dm = NULL;
+	int rc = nbg_dev_alloc(&ds, 24 * (n ? n : 1));
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&dm, 16 * (n ? n : 1));
+	if (rc == NBG_OK) rc = nbg_h2d(ds, stress, 24 * n, NULL);
+	if (rc == NBG_OK) rc = nbg_main_stress_f64(nen, N_elements, ds, dm, NULL);
+	if (rc == NBG_OK) rc = nbg_d2h(main_stress, dm, 16 * n, NULL);
+	if (rc == NBG_OK) rc = nbg_stream_sync(NULL);
+	nbg_dev_free(ds);
+	nbg_dev_free(dm);
+}

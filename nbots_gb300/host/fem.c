@@ -23,7 +23,7 @@ struct nbg_fem {
 	uint64_t nnz;
 	void *stream;
 	/* device arrays */
-	double *nod, *K, *F, *u, *strain, *stress, *E, *Ke, *Fe;
+	double *nod, *K, *F, *u, *strain, *stress, *E, *Ke, *Fe, *main_stress;
 	uint32_t *conn, *row_ptr, *col_idx, *inc_ptr, *inc_elem, *distorted;
 	uint8_t *inc_local, *enabled;
 	unsigned long long *matched;
@@ -270,7 +270,7 @@ void nbg_fem_destroy(nbg_fem_t *f)
 {
 	if (!f)
 		return;
-	void *p[] = {f->nod, f->K, f->F, f->u, f->strain, f->stress, f->E, f->Ke, f->Fe,
+	void *p[] = {f->nod, f->K, f->F, f->u, f->strain, f->stress, f->E, f->Ke, f->Fe, f->main_stress,
 		     f->conn, f->row_ptr, f->col_idx, f->inc_ptr, f->inc_elem, f->distorted,
 		     f->inc_local, f->enabled, f->matched, f->status, f->cg_ws,
 		     f->slice_off, f->bcol, f->b64, f->dinv64, f->b32, f->dinv32, f->blo};
@@ -639,6 +639,17 @@ int nbg_fem_stress(nbg_fem_t *f)
 			      f->has_enabled ? f->enabled : NULL, f->strain, f->stress, f->stream);
 }
 
+int nbg_fem_main_stress(nbg_fem_t *f)
+{
+	if (!f->main_stress) {
+		int rc = nbg_dev_alloc((void **)&f->main_stress,
+				       16 * (size_t)n_gp(f) * (f->m.N_elem ? f->m.N_elem : 1));
+		if (rc != NBG_OK)
+			return rc;
+	}
+	return nbg_main_stress_f64(f->m.nen, f->m.N_elem, f->stress, f->main_stress, f->stream);
+}
+
 void *nbg_fem_device_ptr(nbg_fem_t *f, int what)
 {
 	switch (what) {
@@ -649,6 +660,7 @@ void *nbg_fem_device_ptr(nbg_fem_t *f, int what)
 	case NBG_FEM_U: return f->u;
 	case NBG_FEM_STRAIN: return f->strain;
 	case NBG_FEM_STRESS: return f->stress;
+	case NBG_FEM_MAIN_STRESS: return f->main_stress;
 	case NBG_FEM_E: return f->E;
 	case NBG_FEM_NOD: return f->nod;
 	case NBG_FEM_CONN: return f->conn;
@@ -666,6 +678,7 @@ size_t nbg_fem_bytes(const nbg_fem_t *f, int what)
 	case NBG_FEM_U: return 8 * (size_t)f->N;
 	case NBG_FEM_STRAIN:
 	case NBG_FEM_STRESS: return 8 * 3 * (size_t)n_gp(f) * f->m.N_elem;
+	case NBG_FEM_MAIN_STRESS: return f->main_stress ? 16 * (size_t)n_gp(f) * f->m.N_elem : 0;
 	case NBG_FEM_E: return 8 * (size_t)f->m.N_elem;
 	case NBG_FEM_NOD: return 16 * (size_t)f->m.N_nod;
 	case NBG_FEM_CONN: return 4 * (size_t)f->m.nen * f->m.N_elem;

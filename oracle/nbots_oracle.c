@@ -594,6 +594,20 @@ void orc_stress(const orc_mesh_t *m, const double *E, double nu,
 	}
 }
 
+/* Principal stresses at every Gauss point (pipeline.c:321-340):
+ * mean of the normal stresses plus and minus the radius of Mohr's circle. */
+void orc_main_stress(uint32_t n_points, const double *stress, double *main_stress)
+{
+	for (uint32_t i = 0; i < n_points; i++) {
+		double sx = stress[i * 3], sy = stress[i * 3 + 1], txy = stress[i * 3 + 2];
+		double avg = 0.5 * (sx + sy);
+		double d = sx - sy;
+		double R = sqrt(0.25 * (d * d) + txy * txy);
+		main_stress[i * 2] = avg + R;
+		main_stress[i * 2 + 1] = avg - R;
+	}
+}
+
 void orc_simp_sensitivity(const orc_mesh_t *m, double nu, double thickness,
 			  const double *rho, double penal, double E0, double Emin,
 			  const double *a, const double *b, double *out)

@@ -92,6 +92,7 @@ void orc_stress(const orc_mesh_t *m, const double *E, double nu,
  * Ke0_e is the element stiffness for E = 1 and
  * dE = p rho^(p-1) (E0 - Emin).  a = b = u gives compliance; a = lambda
  * (adjoint) and b = u gives one nodal output.  No counterpart in nbots. */
+void orc_main_stress(uint32_t n_points, const double *stress, double *main_stress);
 void orc_simp_sensitivity(const orc_mesh_t *m, double nu, double thickness,
 			  const double *rho, double penal, double E0, double Emin,
 			  const double *a, const double *b, double *out);

@@ -69,6 +69,8 @@ def lib():
         L.orc_strain.restype = None
         L.orc_stress.argtypes = [vp, vp, f64, vp, vp, vp]
         L.orc_stress.restype = None
+        L.orc_main_stress.argtypes = [u32, vp, vp]
+        L.orc_main_stress.restype = None
         L.orc_simp_sensitivity.argtypes = [vp, f64, f64, vp, f64, f64, f64, vp, vp, vp]
         L.orc_simp_sensitivity.restype = None
         L.orc_wtime.restype = f64
@@ -174,6 +176,15 @@ def strain(fl: Flat, u):
 def stress(fl: Flat, s):
     out = np.zeros_like(s)
     lib().orc_stress(C.byref(fl.mesh), _p(fl.E), fl.p.nu, _p(fl.enabled), _p(s), _p(out))
+    return out
+
+
+def main_stress(stress):
+    """Principal stresses per Gauss point from (sx, sy, txy) triples
+    (pipeline.c:321-340)."""
+    s = np.ascontiguousarray(stress, np.float64)
+    out = np.zeros(2 * (s.size // 3))
+    lib().orc_main_stress(s.size // 3, _p(s), _p(out))
     return out
 
 

@@ -462,6 +462,10 @@ static int run_problem(const char *in, const char *out, uint32_t threads)
 		nb_fem_compute_stress_from_strain(p.N_elem, elem, mat, NB_PLANE_STRESS,
 						  fs, p.enabled, stress);
 		dump("fem_stress", DT_F64, stress, 3 * (uint64_t)ngp * p.N_elem);
+		/* pipeline.c:321-340 */
+		double *mstress = xalloc(8 * 2 * (size_t)ngp * p.N_elem);
+		pipeline_compute_main_stress(stress, mstress, p.N_elem, elem);
+		dump("fem_main_stress", DT_F64, mstress, 2 * (uint64_t)ngp * p.N_elem);
 		nb_material_destroy(mat);
 	}
 	fclose(g_out);
@@ -674,6 +678,11 @@ static int run_utest(const char *txt, uint32_t nvtx, const char *mesh_out,
 	dump("fem_u", DT_F64, disp, 2 * (uint64_t)Nn);
 	dump("fem_strain", DT_F64, strain, 3 * (uint64_t)Ne);
 	dump("fem_stress", DT_F64, stress, 3 * (uint64_t)Ne);
+	{	/* pipeline.c:321-340 (T3: one Gauss point) */
+		double *mstress = xalloc(16 * (size_t)Ne);
+		pipeline_compute_main_stress(stress, mstress, Ne, elem);
+		dump("fem_main_stress", DT_F64, mstress, 2 * (uint64_t)Ne);
+	}
 	double maxd = 0;
 	for (uint32_t i = 0; i < Nn; i++) {
 		double d2 = disp[2 * i] * disp[2 * i] + disp[2 * i + 1] * disp[2 * i + 1];

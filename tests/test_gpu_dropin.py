@@ -91,6 +91,9 @@ def test_fem_entry(G, name):
     # stress from nbots' own strain is bit-exact
     s = ob.stress(d["fem_strain"])
     assert np.array_equal(s.view(np.uint64), d["fem_stress"].view(np.uint64))
+    if "fem_main_stress" in d:
+        ms = ob.main_stress(d["fem_stress"])
+        assert np.array_equal(ms.view(np.uint64), d["fem_main_stress"].view(np.uint64))
     ob.close()
 
 

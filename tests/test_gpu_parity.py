@@ -69,6 +69,8 @@ def test_fem_stages_vs_reference(lib, name):
         s.put(L.FEM_U, d["fem_u"])
         s.strain()
         assert same(s.stress(), d["fem_stress"])
+        if "fem_main_stress" in d:
+            assert same(s.main_stress(), d["fem_main_stress"])
     s.close()
 
 

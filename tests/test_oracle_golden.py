@@ -49,6 +49,9 @@ def test_oracle_stages_bit_exact(golden):
         # nbots' FEM entry itself (one material) gives the same displacements
         assert same(u, d["fem_u"])
         assert same(O.stress(fl, d["fem_strain"]), d["fem_stress"])
+    if "fem_main_stress" in d:
+        # pipeline_compute_main_stress on the reference's own stress
+        assert same(O.main_stress(d["fem_stress"]), d["fem_main_stress"])
 
 
 def test_beam_cantilever_known_answer():
