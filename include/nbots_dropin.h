@@ -136,6 +136,25 @@ void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t 
 void pipeline_compute_main_stress(double *stress, double *main_stress, uint32_t N_elements,
 				  const nb_fem_elem_t *const elem);
 
+/* static_damage2D.h:13-32 (opaque in nbots; accessors below) */
+typedef struct nb_fem_implicit_s nb_fem_implicit_t;
+
+/* static_damage2D.h:34-45, static_damage2D.c:239-470: quasi-static damage
+ * solve, conjugate-gradient branch on the GPU (assembly with damage,
+ * boundary conditions, residual, Jacobi-PCG with Gauss-Seidel fallback,
+ * strain and damage), nbots' log lines appended to `logfile`.  With
+ * enable_Cholesky_solver the call goes to the next definition in link order
+ * (nbots' own) when there is one, else it runs the conjugate-gradient
+ * branch.  Like nbots, every analysis type is computed as plane stress. */
+void nb_fem_compute_2D_Non_Linear_Solid_Mechanics(const nb_mesh2D_t *part,
+						  const nb_fem_elem_t *elem,
+						  const nb_material_t *material,
+						  const nb_bcond_t *bcond, bool enable_self_weight,
+						  double gravity[2], bool enable_Cholesky_solver,
+						  nb_analysis2D_t analysis2D,
+						  nb_analysis2D_params *params2D,
+						  nb_fem_implicit_t *params, const char *logfile);
+
 /* Last error of a drop-in call that nbots would have ended with exit(1)
  * (0 if none); cleared by reading. */
 int nbg_dropin_error(void);
@@ -172,6 +191,20 @@ uint8_t nb_bcond_get_N_dof(const nb_bcond_t *bcond);
 double nb_material_get_elasticity_module(const nb_material_t *mat);
 double nb_material_get_poisson_module(const nb_material_t *mat);
 double nb_material_get_density(const nb_material_t *mat);
+double nb_material_get_traction_limit_stress(const nb_material_t *mat);
+double nb_material_get_fracture_energy(const nb_material_t *mat);
+
+nb_fem_implicit_t *nb_fem_implicit_create(void);
+void nb_fem_implicit_destroy(nb_fem_implicit_t *isparams);
+void nb_fem_implicit_set_N_steps(nb_fem_implicit_t *isparams, uint32_t N_steps);
+void nb_fem_implicit_set_N_max_iter(nb_fem_implicit_t *isparams, uint32_t N_max_iter);
+void nb_fem_implicit_set_N_max_iter_without_enhance(nb_fem_implicit_t *isparams,
+						    uint32_t N_max_iter);
+void nb_fem_implicit_set_residual_tolerance(nb_fem_implicit_t *isparams, double tol);
+uint32_t nb_fem_implicit_get_N_steps(nb_fem_implicit_t *isparams);
+uint32_t nb_fem_implicit_get_N_max_iter(nb_fem_implicit_t *isparams);
+uint32_t nb_fem_implicit_get_N_max_iter_without_enhance(nb_fem_implicit_t *isparams);
+double nb_fem_implicit_get_residual_tolerance(nb_fem_implicit_t *isparams);
 
 uint8_t nb_fem_elem_get_N_nodes(const nb_fem_elem_t *elemtype);
 uint8_t nb_fem_elem_get_N_gpoints(const nb_fem_elem_t *elemtype);

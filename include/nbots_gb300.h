@@ -45,6 +45,8 @@ int nbg_dev_alloc(void **ptr, size_t bytes);
 int nbg_dev_free(void *ptr);
 int nbg_h2d(void *dst, const void *src, size_t bytes, void *stream);
 int nbg_d2h(void *dst, const void *src, size_t bytes, void *stream);
+int nbg_d2d(void *dst, const void *src, size_t bytes, void *stream);
+int nbg_memset(void *dst, int value, size_t bytes, void *stream);
 int nbg_stream_sync(void *stream);
 /* Device-side bounded wait: one thread polls *flag (device memory) until it
  * equals `expect`; after limit_ns nanoseconds it stores NBG_ERR_TIMEOUT in
@@ -65,6 +67,16 @@ int nbg_element_stiffness_f64(uint32_t nen, uint32_t N_elem, const double *nod,
                               double gx, double gy, const uint8_t *enabled,
                               double *Ke, double *Fe, uint32_t *distorted,
                               void *stream);
+
+/* The same with damage[N_gp N_elem] (device, may be NULL): the constitutive
+ * matrix of each Gauss point is scaled by (1 - damage) first
+ * (DMG_pipeline_assemble_system, static_damage2D.c:474-569). */
+int nbg_element_stiffness_damage_f64(uint32_t nen, uint32_t N_elem, const double *nod,
+                                     const uint32_t *conn, const double *E, double nu,
+                                     double thickness, double density, int self_weight,
+                                     double gx, double gy, const uint8_t *enabled,
+                                     const double *damage, double *Ke, double *Fe,
+                                     uint32_t *distorted, void *stream);
 
 /* Row-gather assembly into the CSR of nb_sparse_create(graph, NULL, 2)
  * (sparse.c:20-60) in ascending element order, so K and F equal nbots'
@@ -107,6 +119,52 @@ int nbg_stress_f64(uint32_t nen, uint32_t N_elem, const double *E, double nu,
  * main_stress[2 N_gp N_elem] from stress[3 N_gp N_elem]; bit-exact. */
 int nbg_main_stress_f64(uint32_t nen, uint32_t N_elem, const double *stress,
                         double *main_stress, void *stream);
+
+/* ---------------------------------------------------------------- damage */
+/* Strain, tension damage and damage threshold at every Gauss point
+ * (DMG_pipeline_compute_strain with tension_damage and get_clfd,
+ * static_damage2D.c:134-182, 571-647) for one plane-stress material
+ * (E, nu, traction limit ft, fracture energy gf):
+ * r[id] = max(r_prev[id], tau), damage[id] = 1 - (r0/r) exp(A (1 - r/r0)).
+ * All arrays on the device; distorted as for nbg_element_stiffness_f64. */
+int nbg_strain_damage_f64(uint32_t nen, uint32_t N_elem, const double *nod,
+                          const uint32_t *conn, const double *u, double E, double nu,
+                          double ft, double gf, const double *r_prev, double *r,
+                          double *damage, double *strain, uint32_t *distorted, void *stream);
+/* res = F - K u with nbots' row sums (static_damage2D.c:343-351) and
+ * *norm2 = sum of res^2 (one device double, fixed summation tree).
+ * ws: nbg_residual_workspace_bytes(N) device bytes. */
+size_t nbg_residual_workspace_bytes(uint32_t N);
+int nbg_residual_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+                     const double *K, const double *F, const double *u, double *res,
+                     double *norm2, void *ws, void *stream);
+/* x += dx (device arrays). */
+int nbg_add_to_f64(uint32_t N, double *x, const double *dx, void *stream);
+
+typedef struct {
+    uint32_t niter;   /* sweeps performed */
+    int status;       /* 0, 1 = not converged, NBG_ERR_TIMEOUT, < 0 error */
+    double error;     /* sqrt(sum (b - A x)^2) at the last check */
+} nbg_gs_result_t;
+
+/* Levels of the forward substitution with the lower part of a CSR matrix
+ * (host arrays): every row of level L depends only on rows of levels < L.
+ * lev_rows[N] lists the rows level by level, ascending within a level;
+ * lev_ptr[N+1] delimits the levels; *n_levels is set. */
+int nbg_host_lower_levels(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+                          uint32_t *lev_ptr, uint32_t *lev_rows, uint32_t *n_levels);
+/* nb_sparse_solve_Gauss_Seidel (gauss_seidel.c:14-58) on the device, x as
+ * the initial guess: each sweep forms c = b - (strict upper part) x and
+ * error = |b - A x|^2, stops when error <= tol^2, else solves the lower part
+ * by level-scheduled forward substitution (triangular.c:14-32).  One block
+ * runs the whole solve; it stops with NBG_ERR_TIMEOUT after time_limit_s
+ * seconds (0: no limit).  ws: nbg_gauss_seidel_workspace_bytes(N). */
+size_t nbg_gauss_seidel_workspace_bytes(uint32_t N);
+int nbg_gauss_seidel_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
+                         const double *K, const double *b, double *x, const uint32_t *lev_ptr,
+                         const uint32_t *lev_rows, uint32_t n_levels, uint32_t max_iter,
+                         double tol, double time_limit_s, nbg_gs_result_t *result, void *ws,
+                         void *stream);
 
 /* ------------------------------------------------------------------ SpMV */
 /* y = A x with nbots' per-row left-to-right sum and no FMA
@@ -355,6 +413,33 @@ int nbg_fem_stress(nbg_fem_t *f);
 /* Principal stresses from the current stress (NBG_FEM_MAIN_STRESS). */
 int nbg_fem_main_stress(nbg_fem_t *f);
 
+/* ---------------------------------------------------- quasi-static damage */
+typedef struct {
+    uint32_t iterations;    /* residual evaluations, all load steps */
+    uint32_t cg_solves;     /* conjugate-gradient solves */
+    uint32_t cg_iterations; /* their iterations, summed */
+    uint32_t gs_fallbacks;  /* solves handed to Gauss-Seidel */
+    uint32_t gs_failures;   /* Gauss-Seidel runs that did not converge */
+    double residual;        /* residual norm at the end of the last step */
+} nbg_damage_info_t;
+
+/* nb_fem_compute_2D_Non_Linear_Solid_Mechanics with the conjugate-gradient
+ * solver (static_damage2D.c:239-470) for one plane-stress material with
+ * traction limit ft and fracture energy gf: n_steps load steps with factor
+ * (n+1)/n_steps, each iterating assembly with damage, boundary conditions,
+ * residual F - K u, Jacobi-PCG (x0 = the step's last increment, max N
+ * iterations, absolute tolerance 1e-8; Gauss-Seidel with 60 N sweeps when it
+ * fails), u += du, strain and damage, until the residual is below rtol
+ * (after the first iteration), max_iter iterations, or max_iter_noenh
+ * iterations without a new best residual.  Appends nbots' log lines to
+ * `logfile` (NULL: no log).  Displacements end in NBG_FEM_U, damage in
+ * NBG_FEM_DAMAGE, strain in NBG_FEM_STRAIN.  Returns 0, NBG_DISTORTED, or an
+ * error; Gauss-Seidel stops with NBG_ERR_TIMEOUT after 600 s. */
+int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, double thickness,
+                   double density, int self_weight, const double gravity[2], double ft,
+                   double gf, uint32_t n_steps, uint32_t max_iter, uint32_t max_iter_noenh,
+                   double rtol, const char *logfile, nbg_damage_info_t *info);
+
 /* ------------------------------------------------------------------ SIMP */
 /* SIMP element sensitivities (no counterpart in nbots): with
  * E_e = Emin + rho_e^p (E0 - Emin), out[e] = -p rho_e^(p-1) (E0 - Emin)
@@ -392,6 +477,7 @@ int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double n
 #define NBG_FEM_NOD 8       /* double[2 N_nod] */
 #define NBG_FEM_CONN 9      /* uint32[nen N_elem] */
 #define NBG_FEM_MAIN_STRESS 10  /* double[2 N_gp N_elem] */
+#define NBG_FEM_DAMAGE 11   /* double[N_gp N_elem], after nbg_fem_damage */
 /* Device pointer of one array, and a copy of it to host memory. */
 void *nbg_fem_device_ptr(nbg_fem_t *f, int what);
 size_t nbg_fem_bytes(const nbg_fem_t *f, int what);

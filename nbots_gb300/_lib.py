@@ -48,6 +48,16 @@ class SimpInfo(C.Structure):
                 ("status", C.c_int)]
 
 
+class GsResult(C.Structure):
+    _fields_ = [("niter", C.c_uint32), ("status", C.c_int), ("error", C.c_double)]
+
+
+class DamageInfo(C.Structure):
+    _fields_ = [("iterations", C.c_uint32), ("cg_solves", C.c_uint32),
+                ("cg_iterations", C.c_uint32), ("gs_fallbacks", C.c_uint32),
+                ("gs_failures", C.c_uint32), ("residual", C.c_double)]
+
+
 class Mesh(C.Structure):
     _fields_ = [("nen", u32), ("N_nod", u32), ("N_elem", u32), ("N_edg", u32),
                 ("nod", vp), ("conn", vp), ("edg", vp)]
@@ -71,10 +81,25 @@ SIGS = {
     "nbg_dev_free": ([vp], i32),
     "nbg_h2d": ([vp, vp, sz, vp], i32),
     "nbg_d2h": ([vp, vp, sz, vp], i32),
+    "nbg_d2d": ([vp, vp, sz, vp], i32),
+    "nbg_memset": ([vp, i32, sz, vp], i32),
     "nbg_stream_sync": ([vp], i32),
     "nbg_wait_flag": ([vp, i32, u64, vp, vp], i32),
     "nbg_element_stiffness_f64": ([u32, u32, vp, vp, vp, f64, f64, f64, i32, f64, f64, vp, vp,
                                    vp, vp, vp], i32),
+    "nbg_element_stiffness_damage_f64": ([u32, u32, vp, vp, vp, f64, f64, f64, i32, f64, f64,
+                                          vp, vp, vp, vp, vp, vp], i32),
+    "nbg_strain_damage_f64": ([u32, u32, vp, vp, vp, f64, f64, f64, f64, vp, vp, vp, vp, vp, vp],
+                              i32),
+    "nbg_residual_workspace_bytes": ([u32], sz),
+    "nbg_residual_f64": ([u32, vp, vp, vp, vp, vp, vp, vp, vp, vp], i32),
+    "nbg_add_to_f64": ([u32, vp, vp, vp], i32),
+    "nbg_host_lower_levels": ([u32, vp, vp, vp, vp, C.POINTER(u32)], i32),
+    "nbg_gauss_seidel_workspace_bytes": ([u32], sz),
+    "nbg_gauss_seidel_f64": ([u32, vp, vp, vp, vp, vp, vp, vp, u32, u32, f64, f64,
+                              C.POINTER(GsResult), vp, vp], i32),
+    "nbg_fem_damage": ([vp, vp, f64, f64, f64, f64, i32, vp, f64, f64, u32, u32, u32, f64,
+                        C.c_char_p, C.POINTER(DamageInfo)], i32),
     "nbg_gather_assemble_f64": ([u32, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
                                 i32),
     "nbg_apply_increments_f64": ([u32, vp, vp, vp, vp, vp], i32),
@@ -152,7 +177,7 @@ SIGS = {
 }
 
 (FEM_ROW_PTR, FEM_COL_IDX, FEM_K, FEM_F, FEM_U, FEM_STRAIN, FEM_STRESS, FEM_E, FEM_NOD,
- FEM_CONN, FEM_MAIN_STRESS) = range(11)
+ FEM_CONN, FEM_MAIN_STRESS, FEM_DAMAGE) = range(12)
 CG_JACOBI, CG_RELATIVE = 1, 2
 METHOD_NBOTS, METHOD_FP64, METHOD_MIXED = 0, 1, 2
 PATTERN_SAME = 1

@@ -94,6 +94,7 @@ __global__ void __launch_bounds__(128) k_element(uint32_t N_elem, const double* 
                                                  const double* __restrict__ E, double nu, double th,
                                                  double density, int self_weight, double gx,
                                                  double gy, const uint8_t* __restrict__ enabled,
+                                                 const double* __restrict__ dmg,
                                                  double* __restrict__ Ke, double* __restrict__ Fe,
                                                  uint32_t* distorted) {
     constexpr int ND = 2 * NN;
@@ -137,12 +138,22 @@ __global__ void __launch_bounds__(128) k_element(uint32_t N_elem, const double* 
             return;
         }
         const double wp = Tab<NN>::w(gp);
+        // DMG_pipeline_assemble_system (static_damage2D.c:527-534): each
+        // Gauss point scales D by (1 - damage) first
+        double G0 = D0, G1 = D1, G2 = D2, G3 = D3;
+        if (dmg != nullptr) {
+            const double keep = sub(1.0, dmg[(size_t)e * NGP + gp]);
+            G0 = mul(D0, keep);
+            G1 = mul(D1, keep);
+            G2 = mul(D2, keep);
+            G3 = mul(D3, keep);
+        }
         int o = 0;
 #pragma unroll
         for (int a = 0; a < ND; a++) {
 #pragma unroll
             for (int b = a; b < ND; b++) {
-                double s = bdb<NN>(a, b, dx, dy, D0, D1, D2, D3);
+                double s = bdb<NN>(a, b, dx, dy, G0, G1, G2, G3);
                 k[o] = add(k[o], mul(mul(mul(s, detJ), th), wp));
                 o++;
             }
@@ -395,25 +406,37 @@ extern "C" int nbg_main_stress_f64(uint32_t nen, uint32_t N_elem, const double* 
     return NBG_OK;
 }
 
+extern "C" int nbg_element_stiffness_damage_f64(uint32_t nen, uint32_t N_elem, const double* nod,
+                                                const uint32_t* conn, const double* E, double nu,
+                                                double thickness, double density,
+                                                int self_weight, double gx, double gy,
+                                                const uint8_t* enabled, const double* damage,
+                                                double* Ke, double* Fe, uint32_t* distorted,
+                                                void* stream) {
+    if (N_elem == 0) return NBG_OK;
+    cudaStream_t s = (cudaStream_t)stream;
+    if (nen == 4)
+        k_element<4><<<nblk(N_elem, 128), 128, 0, s>>>(N_elem, nod, conn, E, nu, thickness, density,
+                                                       self_weight, gx, gy, enabled, damage, Ke,
+                                                       Fe, distorted);
+    else if (nen == 3)
+        k_element<3><<<nblk(N_elem, 128), 128, 0, s>>>(N_elem, nod, conn, E, nu, thickness, density,
+                                                       self_weight, gx, gy, enabled, damage, Ke,
+                                                       Fe, distorted);
+    else
+        return NBG_ERR_ARG;
+    NBG_CHECK(cudaGetLastError());
+    return NBG_OK;
+}
+
 extern "C" int nbg_element_stiffness_f64(uint32_t nen, uint32_t N_elem, const double* nod,
                                          const uint32_t* conn, const double* E, double nu,
                                          double thickness, double density, int self_weight,
                                          double gx, double gy, const uint8_t* enabled, double* Ke,
                                          double* Fe, uint32_t* distorted, void* stream) {
-    if (N_elem == 0) return NBG_OK;
-    cudaStream_t s = (cudaStream_t)stream;
-    if (nen == 4)
-        k_element<4><<<nblk(N_elem, 128), 128, 0, s>>>(N_elem, nod, conn, E, nu, thickness, density,
-                                                       self_weight, gx, gy, enabled, Ke, Fe,
-                                                       distorted);
-    else if (nen == 3)
-        k_element<3><<<nblk(N_elem, 128), 128, 0, s>>>(N_elem, nod, conn, E, nu, thickness, density,
-                                                       self_weight, gx, gy, enabled, Ke, Fe,
-                                                       distorted);
-    else
-        return NBG_ERR_ARG;
-    NBG_CHECK(cudaGetLastError());
-    return NBG_OK;
+    return nbg_element_stiffness_damage_f64(nen, N_elem, nod, conn, E, nu, thickness, density,
+                                            self_weight, gx, gy, enabled, nullptr, Ke, Fe,
+                                            distorted, stream);
 }
 
 extern "C" int nbg_gather_assemble_f64(uint32_t nen, uint32_t N_nod, uint32_t N_elem,

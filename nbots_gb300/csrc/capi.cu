@@ -57,6 +57,18 @@ extern "C" int nbg_d2h(void* dst, const void* src, size_t bytes, void* stream) {
     return NBG_OK;
 }
 
+extern "C" int nbg_d2d(void* dst, const void* src, size_t bytes, void* stream) {
+    if (bytes == 0) return NBG_OK;
+    NBG_CHECK(cudaMemcpyAsync(dst, src, bytes, cudaMemcpyDeviceToDevice, (cudaStream_t)stream));
+    return NBG_OK;
+}
+
+extern "C" int nbg_memset(void* dst, int value, size_t bytes, void* stream) {
+    if (bytes == 0) return NBG_OK;
+    NBG_CHECK(cudaMemsetAsync(dst, value, bytes, (cudaStream_t)stream));
+    return NBG_OK;
+}
+
 extern "C" int nbg_stream_sync(void* stream) {
     NBG_CHECK(cudaStreamSynchronize((cudaStream_t)stream));
     return NBG_OK;

@@ -77,6 +77,9 @@ def libs():
         G.nb_fem_compute_stress_from_strain.restype = None
         G.pipeline_compute_main_stress.argtypes = [vp, vp, u32, vp]
         G.pipeline_compute_main_stress.restype = None
+        G.nb_fem_compute_2D_Non_Linear_Solid_Mechanics.argtypes = [
+            vp, vp, vp, vp, b8, vp, b8, C.c_int, C.POINTER(Params2D), vp, C.c_char_p]
+        G.nb_fem_compute_2D_Non_Linear_Solid_Mechanics.restype = None
         G.nbg_dropin_error.restype = C.c_int
         H.nbh_mesh2D_create.argtypes = [u32, u32, vp, u32, vp, u32, vp, u32, vp, u32, vp, vp]
         H.nbh_mesh2D_create.restype = vp
@@ -95,6 +98,13 @@ def libs():
         for n in ("elasticity", "poisson"):
             getattr(H, f"nb_material_set_{n}_module").argtypes = [vp, f64]
         H.nb_material_set_density.argtypes = [vp, f64]
+        H.nb_material_set_traction_limit_stress.argtypes = [vp, f64]
+        H.nb_material_set_fracture_energy.argtypes = [vp, f64]
+        H.nb_fem_implicit_create.restype = vp
+        H.nb_fem_implicit_destroy.argtypes = [vp]
+        for n in ("N_steps", "N_max_iter", "N_max_iter_without_enhance"):
+            getattr(H, f"nb_fem_implicit_set_{n}").argtypes = [vp, u32]
+        H.nb_fem_implicit_set_residual_tolerance.argtypes = [vp, f64]
         H.nb_fem_elem_create.argtypes = [C.c_int]
         H.nb_fem_elem_create.restype = vp
         H.nb_fem_elem_destroy.argtypes = [vp]
@@ -177,6 +187,29 @@ class NbotsObjects:
                                                  None if en is None else en.ctypes.data,
                                                  u.ctypes.data, strain.ctypes.data)
         return st, u, strain
+
+    def damage(self, ft, gf, n_steps, max_iter, max_iter_noenh, rtol, logfile):
+        """nb_fem_compute_2D_Non_Linear_Solid_Mechanics through the drop-in
+        symbol (conjugate-gradient branch); the log is appended to
+        `logfile`."""
+        G, H = libs()
+        p = self.p
+        H.nb_material_set_traction_limit_stress(self.mat, ft)
+        H.nb_material_set_fracture_energy(self.mat, gf)
+        ip = H.nb_fem_implicit_create()
+        H.nb_fem_implicit_set_N_steps(ip, n_steps)
+        H.nb_fem_implicit_set_N_max_iter(ip, max_iter)
+        H.nb_fem_implicit_set_N_max_iter_without_enhance(ip, max_iter_noenh)
+        H.nb_fem_implicit_set_residual_tolerance(ip, rtol)
+        grav = (f64 * 2)(*p.gravity)
+        params = Params2D(p.thickness, 0.0, b"\0")
+        try:
+            G.nb_fem_compute_2D_Non_Linear_Solid_Mechanics(
+                self.mesh, self.elem, self.mat, self.bcond, bool(p.self_weight),
+                C.addressof(grav), False, 0, C.byref(params), ip, str(logfile).encode())
+        finally:
+            H.nb_fem_implicit_destroy(ip)
+        return G.nbg_dropin_error()
 
     def stress(self, strain):
         G, _ = libs()

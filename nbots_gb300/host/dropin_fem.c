@@ -9,6 +9,8 @@
  * evaluates them (set_bconditions.c:63-260): segment nodes, vertex nodes for
  * Dirichlet, and (0,0) for Neumann vertex loads.
  */
+#define _GNU_SOURCE
+#include <dlfcn.h>
 #include <stdlib.h>
 #include <string.h>
 
@@ -277,4 +279,61 @@ void pipeline_compute_main_stress(double *stress, double *main_stress, uint32_t 
 	if (rc == NBG_OK) rc = nbg_stream_sync(NULL);
 	nbg_dev_free(ds);
 	nbg_dev_free(dm);
+}
+
+void nbg_dropin_record_error(int e);
+
+typedef void (*nonlinear_fn)(const nb_mesh2D_t *, const nb_fem_elem_t *, const nb_material_t *,
+			     const nb_bcond_t *, bool, double[2], bool, nb_analysis2D_t,
+			     nb_analysis2D_params *, nb_fem_implicit_t *, const char *);
+
+void nb_fem_compute_2D_Non_Linear_Solid_Mechanics(const nb_mesh2D_t *part,
+						  const nb_fem_elem_t *elem,
+						  const nb_material_t *material,
+						  const nb_bcond_t *bcond, bool enable_self_weight,
+						  double gravity[2], bool enable_Cholesky_solver,
+						  nb_analysis2D_t analysis2D,
+						  nb_analysis2D_params *params2D,
+						  nb_fem_implicit_t *params, const char *logfile)
+{
+	if (enable_Cholesky_solver) {
+		/* the direct-solver branch is nbots' own */
+		nonlinear_fn next = (nonlinear_fn)dlsym(
+			RTLD_NEXT, "nb_fem_compute_2D_Non_Linear_Solid_Mechanics");
+		if (next) {
+			next(part, elem, material, bcond, enable_self_weight, gravity, true,
+			     analysis2D, params2D, params, logfile);
+			return;
+		}
+	}
+	const uint32_t nen = nb_fem_elem_get_N_nodes(elem);
+	if (nen != 3 && nen != 4) {
+		nbg_dropin_record_error(NBG_ERR_ARG);
+		return;
+	}
+	host_problem_t h;
+	memset(&h, 0, sizeof(h));
+	nbg_fem_t *f = NULL;
+	int rc = read_mesh(part, nen, &h);
+	if (rc == NBG_OK)
+		rc = read_bcond(part, bcond, &h);
+	if (rc == NBG_OK)
+		rc = nbg_fem_create(&f, &h.m, NULL);
+	if (rc == NBG_OK) {
+		double g2[2] = {gravity ? gravity[0] : 0.0, gravity ? gravity[1] : 0.0};
+		nbg_bcs_t b = {h.vtx, h.N_sgm, h.sgm_ptr, h.sgm_nodes, h.N_bc, h.bc};
+		nbg_damage_info_t info;
+		rc = nbg_fem_damage(f, &b, nb_material_get_elasticity_module(material),
+				    nb_material_get_poisson_module(material), params2D->thickness,
+				    nb_material_get_density(material), enable_self_weight, g2,
+				    nb_material_get_traction_limit_stress(material),
+				    nb_material_get_fracture_energy(material),
+				    nb_fem_implicit_get_N_steps(params),
+				    nb_fem_implicit_get_N_max_iter(params),
+				    nb_fem_implicit_get_N_max_iter_without_enhance(params),
+				    nb_fem_implicit_get_residual_tolerance(params), logfile, &info);
+	}
+	nbg_dropin_record_error(rc);
+	nbg_fem_destroy(f);
+	free_problem(&h);
 }

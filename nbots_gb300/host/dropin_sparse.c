@@ -38,6 +38,13 @@ int nbg_dropin_error(void)
 	return e;
 }
 
+/* Records the status of a drop-in entry that returns void in nbots. */
+void nbg_dropin_record_error(int e)
+{
+	if (e)
+		g_err = e;
+}
+
 static void reg_add(const nb_sparse_t *A, double *v, uint32_t *ix, uint64_t nnz)
 {
 	pthread_mutex_lock(&g_lock);

@@ -17,29 +17,7 @@
 
 #include "nbots_gb300.h"
 
-struct nbg_fem {
-	nbg_mesh_t m;
-	uint32_t N;        /* dofs */
-	uint64_t nnz;
-	void *stream;
-	/* device arrays */
-	double *nod, *K, *F, *u, *strain, *stress, *E, *Ke, *Fe, *main_stress;
-	uint32_t *conn, *row_ptr, *col_idx, *inc_ptr, *inc_elem, *distorted;
-	uint8_t *inc_local, *enabled;
-	unsigned long long *matched;
-	int *status;
-	double nu;
-	int has_enabled;
-	void *cg_ws;
-	size_t cg_ws_bytes;
-	/* 2x2-block SELL copy (bsr.cu), filled from K on demand */
-	int bsr_ok;
-	nbg_bsr_t bsr;
-	uint32_t *slice_off, *bcol;
-	double *b64, *dinv64;
-	float *b32, *dinv32;
-	uint16_t *blo;
-};
+#include "fem_internal.h"
 
 static int cmp_u32(const void *a, const void *b)
 {
@@ -271,6 +249,7 @@ void nbg_fem_destroy(nbg_fem_t *f)
 	if (!f)
 		return;
 	void *p[] = {f->nod, f->K, f->F, f->u, f->strain, f->stress, f->E, f->Ke, f->Fe, f->main_stress,
+		     f->damage,
 		     f->conn, f->row_ptr, f->col_idx, f->inc_ptr, f->inc_elem, f->distorted,
 		     f->inc_local, f->enabled, f->matched, f->status, f->cg_ws,
 		     f->slice_off, f->bcol, f->b64, f->dinv64, f->b32, f->dinv32, f->blo};
@@ -378,6 +357,14 @@ int nbg_fem_assemble(nbg_fem_t *f, const double *E, double nu, double thickness,
 		     double density, int self_weight, const double gravity[2],
 		     const uint8_t *enabled)
 {
+	return nbg_fem_assemble_dev_damage(f, E, nu, thickness, density, self_weight, gravity,
+					   enabled, NULL);
+}
+
+int nbg_fem_assemble_dev_damage(nbg_fem_t *f, const double *E, double nu, double thickness,
+				double density, int self_weight, const double gravity[2],
+				const uint8_t *enabled, const double *damage)
+{
 	int rc = NBG_OK;
 	const size_t ne = f->m.N_elem, nen = f->m.nen, nd = 2 * nen;
 	if (!f->Ke) {
@@ -394,10 +381,10 @@ int nbg_fem_assemble(nbg_fem_t *f, const double *E, double nu, double thickness,
 	TRY(nbg_h2d(f->distorted, &init, 4, f->stream));
 	TRY(nbg_h2d(f->matched, &zero, 8, f->stream));
 	double gx = gravity ? gravity[0] : 0.0, gy = gravity ? gravity[1] : 0.0;
-	TRY(nbg_element_stiffness_f64((uint32_t)nen, (uint32_t)ne, f->nod, f->conn, f->E, nu,
-				      thickness, density, self_weight, gx, gy,
-				      enabled ? f->enabled : NULL, f->Ke, f->Fe, f->distorted,
-				      f->stream));
+	TRY(nbg_element_stiffness_damage_f64((uint32_t)nen, (uint32_t)ne, f->nod, f->conn, f->E,
+					     nu, thickness, density, self_weight, gx, gy,
+					     enabled ? f->enabled : NULL, damage, f->Ke, f->Fe,
+					     f->distorted, f->stream));
 	uint32_t dist_h = 0;
 	TRY(nbg_d2h(&dist_h, f->distorted, 4, f->stream));
 	TRY(nbg_stream_sync(f->stream));
@@ -523,8 +510,7 @@ fail:
 	return rc;
 }
 
-int nbg_fem_solve(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
-		  nbg_cg_result_t *res)
+int nbg_fem_cg_workspace(nbg_fem_t *f)
 {
 	int rc = NBG_OK;
 	size_t need = nbg_cg_workspace_bytes(f->N);
@@ -535,6 +521,16 @@ int nbg_fem_solve(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
 		TRY(nbg_dev_alloc(&f->cg_ws, need));
 		f->cg_ws_bytes = need;
 	}
+fail:
+	return rc;
+}
+
+int nbg_fem_solve(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
+		  nbg_cg_result_t *res)
+{
+	int rc = nbg_fem_cg_workspace(f);
+	if (rc != NBG_OK)
+		return rc;
 	double *zero = calloc(f->N ? f->N : 1, sizeof(double));
 	if (!zero)
 		return NBG_ERR_NOMEM;
@@ -546,8 +542,6 @@ int nbg_fem_solve(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
 		return rc;
 	return nbg_cg_f64(f->N, f->row_ptr, f->col_idx, f->K, f->F, f->u, max_iter, tol, flags,
 			  res, f->cg_ws, f->cg_ws_bytes, f->stream);
-fail:
-	return rc;
 }
 
 int nbg_fem_block_layout(nbg_fem_t *f, nbg_bsr_t *out)
@@ -661,6 +655,7 @@ void *nbg_fem_device_ptr(nbg_fem_t *f, int what)
 	case NBG_FEM_STRAIN: return f->strain;
 	case NBG_FEM_STRESS: return f->stress;
 	case NBG_FEM_MAIN_STRESS: return f->main_stress;
+	case NBG_FEM_DAMAGE: return f->damage;
 	case NBG_FEM_E: return f->E;
 	case NBG_FEM_NOD: return f->nod;
 	case NBG_FEM_CONN: return f->conn;
@@ -679,6 +674,7 @@ size_t nbg_fem_bytes(const nbg_fem_t *f, int what)
 	case NBG_FEM_STRAIN:
 	case NBG_FEM_STRESS: return 8 * 3 * (size_t)n_gp(f) * f->m.N_elem;
 	case NBG_FEM_MAIN_STRESS: return f->main_stress ? 16 * (size_t)n_gp(f) * f->m.N_elem : 0;
+	case NBG_FEM_DAMAGE: return f->damage ? 8 * (size_t)n_gp(f) * f->m.N_elem : 0;
 	case NBG_FEM_E: return 8 * (size_t)f->m.N_elem;
 	case NBG_FEM_NOD: return 16 * (size_t)f->m.N_nod;
 	case NBG_FEM_CONN: return 4 * (size_t)f->m.nen * f->m.N_elem;

@@ -1,0 +1,42 @@
+/*
+ * The device-resident FEM system shared by fem.c (elastic path) and
+ * damage.c (quasi-static damage path).  Private to the host library.
+ */
+#ifndef NBG_FEM_INTERNAL_H
+#define NBG_FEM_INTERNAL_H
+
+#include "nbots_gb300.h"
+
+struct nbg_fem {
+	nbg_mesh_t m;
+	uint32_t N;        /* dofs */
+	uint64_t nnz;
+	void *stream;
+	/* device arrays */
+	double *nod, *K, *F, *u, *strain, *stress, *E, *Ke, *Fe, *main_stress;
+	double *damage;    /* per Gauss point, owned by the damage solve */
+	uint32_t *conn, *row_ptr, *col_idx, *inc_ptr, *inc_elem, *distorted;
+	uint8_t *inc_local, *enabled;
+	unsigned long long *matched;
+	int *status;
+	double nu;
+	int has_enabled;
+	void *cg_ws;
+	size_t cg_ws_bytes;
+	/* 2x2-block SELL copy (bsr.cu), filled from K on demand */
+	int bsr_ok;
+	nbg_bsr_t bsr;
+	uint32_t *slice_off, *bcol;
+	double *b64, *dinv64;
+	float *b32, *dinv32;
+	uint16_t *blo;
+};
+
+/* Assembly with an optional device array of damage per Gauss point. */
+int nbg_fem_assemble_dev_damage(nbg_fem_t *f, const double *E, double nu, double thickness,
+				double density, int self_weight, const double gravity[2],
+				const uint8_t *enabled, const double *damage);
+/* Grow f's CG workspace to what nbg_cg_f64 needs for f->N dofs. */
+int nbg_fem_cg_workspace(nbg_fem_t *f);
+
+#endif

@@ -262,7 +262,7 @@ void nb_bcond_iter_get_val(const nb_bcond_iter_t *it, uint8_t N_dof, double *x, 
 
 /* ------------------------------------------------------------- material */
 struct nb_material_s {
-	double E, nu, density;
+	double E, nu, density, ft, gf;
 };
 
 nb_material_t *nb_material_create(void) { return calloc(1, sizeof(nb_material_t)); }
@@ -273,6 +273,40 @@ void nb_material_set_density(nb_material_t *m, double v) { m->density = v; }
 double nb_material_get_elasticity_module(const nb_material_t *m) { return m->E; }
 double nb_material_get_poisson_module(const nb_material_t *m) { return m->nu; }
 double nb_material_get_density(const nb_material_t *m) { return m->density; }
+void nb_material_set_traction_limit_stress(nb_material_t *m, double v) { m->ft = v; }
+void nb_material_set_fracture_energy(nb_material_t *m, double v) { m->gf = v; }
+double nb_material_get_traction_limit_stress(const nb_material_t *m) { return m->ft; }
+double nb_material_get_fracture_energy(const nb_material_t *m) { return m->gf; }
+
+/* ------------------------------------------- implicit-solve parameters */
+/* static_damage2D.c:27-125: four plain fields behind accessors */
+struct nb_fem_implicit_s {
+	uint32_t N_steps, N_max_iter, N_max_iter_without_enhance;
+	double residual_tolerance;
+};
+
+nb_fem_implicit_t *nb_fem_implicit_create(void) { return calloc(1, sizeof(nb_fem_implicit_t)); }
+void nb_fem_implicit_destroy(nb_fem_implicit_t *p) { free(p); }
+void nb_fem_implicit_set_N_steps(nb_fem_implicit_t *p, uint32_t v) { p->N_steps = v; }
+void nb_fem_implicit_set_N_max_iter(nb_fem_implicit_t *p, uint32_t v) { p->N_max_iter = v; }
+void nb_fem_implicit_set_N_max_iter_without_enhance(nb_fem_implicit_t *p, uint32_t v)
+{
+	p->N_max_iter_without_enhance = v;
+}
+void nb_fem_implicit_set_residual_tolerance(nb_fem_implicit_t *p, double v)
+{
+	p->residual_tolerance = v;
+}
+uint32_t nb_fem_implicit_get_N_steps(nb_fem_implicit_t *p) { return p->N_steps; }
+uint32_t nb_fem_implicit_get_N_max_iter(nb_fem_implicit_t *p) { return p->N_max_iter; }
+uint32_t nb_fem_implicit_get_N_max_iter_without_enhance(nb_fem_implicit_t *p)
+{
+	return p->N_max_iter_without_enhance;
+}
+double nb_fem_implicit_get_residual_tolerance(nb_fem_implicit_t *p)
+{
+	return p->residual_tolerance;
+}
 
 /* -------------------------------------------------------------- element */
 struct nb_fem_elem_s {

@@ -7,6 +7,8 @@
 #include <stdlib.h>
 #include <string.h>
 #include <math.h>
+#include <stdarg.h>
+#include <stdio.h>
 #include <time.h>
 #ifdef _OPENMP
 #include <omp.h>
@@ -219,9 +221,26 @@ static void derivatives(const tab_t *t, int gp, const double Jinv[4],
 /* assemble_element + integrate_elemental_system + pipeline_sum_gauss_point
  * (pde_bot/finite_element/solid_mechanics/pipeline.c:83-230), without the
  * mass matrix (the FEM entry passes M = NULL). */
+static int element_dmg(const orc_mesh_t *m, uint32_t e, double E, double nu,
+		       double thickness, double density, int self_weight,
+		       const double gravity[2], int enabled, const double *dmg,
+		       double *Ke, double *Fe);
+
 int orc_element(const orc_mesh_t *m, uint32_t e, double E, double nu,
 		double thickness, double density, int self_weight,
 		const double gravity[2], int enabled, double *Ke, double *Fe)
+{
+	return element_dmg(m, e, E, nu, thickness, density, self_weight, gravity, enabled,
+			   NULL, Ke, Fe);
+}
+
+/* With dmg != NULL, the constitutive matrix of Gauss point gp is scaled by
+ * (1 - dmg[gp]) first (DMG_pipeline_assemble_system,
+ * static_damage2D.c:527-534). */
+static int element_dmg(const orc_mesh_t *m, uint32_t e, double E, double nu,
+		       double thickness, double density, int self_weight,
+		       const double gravity[2], int enabled, const double *dmg,
+		       double *Ke, double *Fe)
 {
 	tab_t t = table(m->nen);
 	int n2 = 2 * t.nn;
@@ -240,6 +259,10 @@ int orc_element(const orc_mesh_t *m, uint32_t e, double E, double nu,
 	memset(Fe, 0, sizeof(double) * n2);
 	double dx[4], dy[4];
 	for (int gp = 0; gp < t.ngp; gp++) {
+		double Dg[4] = {D[0], D[1], D[2], D[3]};
+		if (dmg)
+			for (int k = 0; k < 4; k++)
+				Dg[k] *= (1.0 - dmg[gp]);
 		double Jinv[4];
 		double detJ = jacobian(m, &t, e, gp, Jinv);
 		if (detJ < 0)
@@ -250,16 +273,16 @@ int orc_element(const orc_mesh_t *m, uint32_t e, double E, double nu,
 			double Ni = t.N[i * t.ngp + gp];
 			for (int j = 0; j < t.nn; j++) {
 				Ke[(2 * i) * n2 + 2 * j] +=
-					(dx[i] * dx[j] * D[0] + dy[i] * dy[j] * D[3]) *
+					(dx[i] * dx[j] * Dg[0] + dy[i] * dy[j] * Dg[3]) *
 					detJ * thickness * wp;
 				Ke[(2 * i) * n2 + 2 * j + 1] +=
-					(dx[i] * dy[j] * D[1] + dy[i] * dx[j] * D[3]) *
+					(dx[i] * dy[j] * Dg[1] + dy[i] * dx[j] * Dg[3]) *
 					detJ * thickness * wp;
 				Ke[(2 * i + 1) * n2 + 2 * j] +=
-					(dy[i] * dx[j] * D[1] + dx[i] * dy[j] * D[3]) *
+					(dy[i] * dx[j] * Dg[1] + dx[i] * dy[j] * Dg[3]) *
 					detJ * thickness * wp;
 				Ke[(2 * i + 1) * n2 + 2 * j + 1] +=
-					(dy[i] * dy[j] * D[2] + dx[i] * dx[j] * D[3]) *
+					(dy[i] * dy[j] * Dg[2] + dx[i] * dx[j] * Dg[3]) *
 					detJ * thickness * wp;
 			}
 			double integral = Ni * detJ * thickness * wp;
@@ -634,4 +657,224 @@ void orc_simp_sensitivity(const orc_mesh_t *m, double nu, double thickness,
 		double dE = penal * pow(rho[e], penal - 1.0) * (E0 - Emin);
 		out[e] = -dE * s;
 	}
+}
+
+/* ------------------------------------------------------------ damage model */
+#define DMG_MAX(a, b) (((a) > (b)) ? (a) : (b))   /* static_damage2D.c:24 */
+
+/* nb_sparse_forward_solve (solver_bot/sparse/solvers/triangular.c:14-32) */
+static void forward_solve(uint32_t N, const uint32_t *rp, const uint32_t *ci, const double *K,
+			  const double *b, double *x)
+{
+	for (uint32_t i = 0; i < N; i++) {
+		x[i] = b[i];
+		uint32_t q = rp[i];
+		while (ci[q] < i) {
+			x[i] -= K[q] * x[ci[q]];
+			q++;
+		}
+		if (ci[rp[i + 1] - 1] == i)
+			x[i] /= K[rp[i + 1] - 1];
+		else
+			x[i] /= K[bsearch_row(ci + rp[i], rp[i + 1] - rp[i], i) + rp[i]];
+	}
+}
+
+/* nb_sparse_solve_Gauss_Seidel (solver_bot/sparse/solvers/gauss_seidel.c:14-58),
+ * one thread */
+int orc_gauss_seidel(uint32_t N, const uint32_t *rp, const uint32_t *ci, const double *K,
+		     const double *b, double *x, uint32_t max_iter, double tol,
+		     uint32_t *niter, double *tol_reached)
+{
+	double *c = calloc(N ? N : 1, sizeof(double));
+	uint32_t k = 0;
+	double error = 1e10;
+	while (k < max_iter) {
+		error = 0;
+		for (uint32_t i = 0; i < N; i++) {
+			c[i] = b[i];
+			double error_i = b[i];
+			for (uint32_t j = rp[i]; j < rp[i + 1]; j++) {
+				error_i -= K[j] * x[ci[j]];
+				if (ci[j] > i)
+					c[i] -= K[j] * x[ci[j]];
+			}
+			error += error_i * error_i;
+		}
+		if (error <= tol * tol)
+			break;
+		forward_solve(N, rp, ci, K, c, x);
+		k++;
+	}
+	free(c);
+	if (niter) *niter = k;
+	if (tol_reached) *tol_reached = sqrt(error);
+	return error > tol * tol ? 1 : 0;
+}
+
+/* tension_damage (static_damage2D.c:134-182) at one Gauss point */
+double orc_tension_damage(double E, double nu, double ft, double gf, const double *strain,
+			  double r_prev, double *r, double clfd)
+{
+	double D[4];
+	plane_stress(D, E, nu);
+	double es[3];
+	es[0] = D[0] * strain[0] + D[1] * strain[1];
+	es[1] = D[1] * strain[0] + D[2] * strain[1];
+	es[2] = D[3] * strain[2];
+	double avg = 0.5 * (es[0] + es[1]);
+	double d = es[0] - es[1];
+	double R = sqrt(0.25 * (d * d) + es[2] * es[2]);
+	double p1 = DMG_MAX(0, avg + R);
+	double p2 = DMG_MAX(0, avg - R);
+	double det = D[0] * D[2] - D[1] * D[1];
+	double id11 = D[2] / det, id12 = -D[1] / det, id22 = D[0] / det;
+	double sTs = id11 * (p1 * p1) + 2 * id12 * p1 * p2 + id22 * (p2 * p2);
+	double tau = sqrt(sTs);
+	double r0 = ft / sqrt(E);
+	*r = DMG_MAX(r_prev, tau);
+	double div = (gf / clfd) * (E / (ft * ft));
+	double A = 1.0 / (div - 0.5);
+	return 1.0 - (r0 / *r) * exp(A * (1.0 - (*r / r0)));
+}
+
+/* get_clfd (static_damage2D.c:633-647): sqrt of twice the area of the
+ * triangle of the element's first three nodes */
+static double clfd_of(const orc_mesh_t *m, uint32_t e)
+{
+	const uint32_t *c = m->conn + (size_t)e * m->nen;
+	double x1 = m->nod[2 * c[0]], y1 = m->nod[2 * c[0] + 1];
+	double x2 = m->nod[2 * c[1]], y2 = m->nod[2 * c[1] + 1];
+	double x3 = m->nod[2 * c[2]], y3 = m->nod[2 * c[2] + 1];
+	return sqrt((x2 - x1) * (y3 - y1) - (y2 - y1) * (x3 - x1));
+}
+
+static void logf_(char *log, size_t cap, size_t *len, const char *fmt, ...)
+{
+	va_list ap;
+	va_start(ap, fmt);
+	int n = vsnprintf(log + *len, *len < cap ? cap - *len : 0, fmt, ap);
+	va_end(ap);
+	if (n > 0)
+		*len = *len + (size_t)n < cap ? *len + (size_t)n : cap;
+}
+
+/* nb_fem_compute_2D_Non_Linear_Solid_Mechanics (static_damage2D.c:239-470)
+ * with the conjugate-gradient path (enable_Cholesky_solver false), one
+ * material, all elements enabled.  Writes nbots' log text into `log`
+ * (cap bytes, NUL-terminated) and the final displacements and damage (N_gp
+ * per element).  Returns how many solves fell back to Gauss-Seidel. */
+int orc_damage_solve(const orc_mesh_t *m, const orc_bcs_t *b, double E, double nu,
+		     double thickness, double density, int self_weight, const double gravity[2],
+		     double ft, double gf, uint32_t n_steps, uint32_t max_iter,
+		     uint32_t max_iter_noenh, double rtol, char *log, size_t cap,
+		     double *u_out, double *damage_out)
+{
+	tab_t t = table(m->nen);
+	const uint32_t N = 2 * m->N_nod, ngp = (uint32_t)t.ngp, nn = m->nen, n2 = 2 * nn;
+	const size_t npt = (size_t)ngp * m->N_elem;
+	size_t len = 0;
+	if (cap) log[0] = 0;
+	uint32_t *rp = malloc(((size_t)N + 1) * sizeof(uint32_t));
+	orc_pattern(m, rp, NULL);
+	uint32_t *ci = malloc(((size_t)rp[N] + 1) * sizeof(uint32_t));
+	orc_pattern(m, rp, ci);
+	double *K = calloc(rp[N] + 1, sizeof(double));
+	double *disp = calloc(N, sizeof(double)), *F = calloc(N, sizeof(double));
+	double *P = calloc(N, sizeof(double)), *res = calloc(N, sizeof(double));
+	double *du = calloc(N, sizeof(double));
+	double *strain = calloc(3 * npt, sizeof(double)), *dmg = calloc(npt, sizeof(double));
+	double *r = malloc(npt * sizeof(double)), *r_prev = malloc(npt * sizeof(double));
+	const double r0 = ft / sqrt(E);
+	for (size_t i = 0; i < npt; i++)
+		r[i] = r0;
+	int n_gs = 0;
+	logf_(log, cap, &len, "FEM: Damage Model\n");
+	for (uint32_t n = 0; n < n_steps; n++) {
+		logf_(log, cap, &len, "  [ Load step %i]\n", n + 1);
+		memcpy(r_prev, r, npt * sizeof(double));
+		memset(du, 0, N * sizeof(double));
+		double residual_norm = 1, residual_best = 0;
+		uint32_t iter = 0, noenh = 0;
+		for (;;) {
+			/* DMG_pipeline_assemble_system (static_damage2D.c:474-569) */
+			memset(K, 0, rp[N] * sizeof(double));
+			memset(F, 0, N * sizeof(double));
+			double Ke[64], Fe[8];
+			for (uint32_t e = 0; e < m->N_elem; e++) {
+				if (element_dmg(m, e, E, nu, thickness, density, self_weight, gravity, 1,
+						dmg + (size_t)e * ngp, Ke, Fe))
+					break;
+				for (uint32_t i = 0; i < nn; i++) {
+					uint32_t v1 = m->conn[e * nn + i];
+					for (uint32_t j = 0; j < nn; j++) {
+						uint32_t v2 = m->conn[e * nn + j];
+						*slot(rp, ci, K, 2 * v1, 2 * v2) += Ke[(2 * i) * n2 + 2 * j];
+						*slot(rp, ci, K, 2 * v1 + 1, 2 * v2) += Ke[(2 * i + 1) * n2 + 2 * j];
+						*slot(rp, ci, K, 2 * v1, 2 * v2 + 1) += Ke[(2 * i) * n2 + 2 * j + 1];
+						*slot(rp, ci, K, 2 * v1 + 1, 2 * v2 + 1) +=
+							Ke[(2 * i + 1) * n2 + 2 * j + 1];
+					}
+					F[2 * v1] += Fe[2 * i];
+					F[2 * v1 + 1] += Fe[2 * i + 1];
+				}
+			}
+			double factor = (n + 1.0) / (double)n_steps;
+			orc_set_bconditions(m, b, rp, ci, K, F, factor);
+			orc_spmv(N, rp, ci, K, disp, P, 1);
+			residual_norm = 0;
+			for (uint32_t i = 0; i < N; i++) {
+				res[i] = F[i] - P[i];
+				residual_norm += res[i] * res[i];
+			}
+			residual_norm = sqrt(residual_norm);
+			if (iter == 0) {
+				residual_best = residual_norm;
+			} else {
+				if (residual_norm < residual_best) {
+					residual_best = residual_norm;
+					noenh = 0;
+				} else {
+					noenh += 1;
+				}
+			}
+			if ((residual_norm < rtol && iter > 0) || iter >= max_iter ||
+			    noenh >= max_iter_noenh) {
+				logf_(log, cap, &len, "    [%i: Residual: %e ]\n", iter, residual_norm);
+				break;
+			}
+			uint32_t its = 0;
+			double err = 0.0;
+			int st = orc_cg_jacobi(N, rp, ci, K, res, du, N, 1e-8, &its, &err, 1);
+			if (st != 0) {
+				n_gs++;
+				st = orc_gauss_seidel(N, rp, ci, K, res, du, 60 * N, 1e-8, &its, &err);
+				if (st != 0) {
+					logf_(log, cap, &len,
+					      "    [Conjugate Gradient (p. Jacobi) and Gauss-Seidel fails.]\n");
+					logf_(log, cap, &len, "      [Gauss-Seidel iterations: %u]\n", its);
+					logf_(log, cap, &len, "      [Gauss-Seidel error: %e ]\n", err);
+				}
+			}
+			logf_(log, cap, &len, "    [%i: Residual: %e]\n", iter, residual_norm);
+			for (uint32_t i = 0; i < N; i++)
+				disp[i] += du[i];
+			/* DMG_pipeline_compute_strain (static_damage2D.c:571-631) */
+			orc_strain(m, disp, strain);
+			for (uint32_t e = 0; e < m->N_elem; e++) {
+				double cl = clfd_of(m, e);
+				for (uint32_t g = 0; g < ngp; g++) {
+					size_t idx = (size_t)e * ngp + g;
+					dmg[idx] = orc_tension_damage(E, nu, ft, gf, strain + 3 * idx,
+								      r_prev[idx], r + idx, cl);
+				}
+			}
+			iter++;
+		}
+	}
+	if (u_out) memcpy(u_out, disp, N * sizeof(double));
+	if (damage_out) memcpy(damage_out, dmg, npt * sizeof(double));
+	free(rp); free(ci); free(K); free(disp); free(F); free(P); free(res); free(du);
+	free(strain); free(dmg); free(r); free(r_prev);
+	return n_gs;
 }

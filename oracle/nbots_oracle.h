@@ -93,6 +93,16 @@ void orc_stress(const orc_mesh_t *m, const double *E, double nu,
  * dE = p rho^(p-1) (E0 - Emin).  a = b = u gives compliance; a = lambda
  * (adjoint) and b = u gives one nodal output.  No counterpart in nbots. */
 void orc_main_stress(uint32_t n_points, const double *stress, double *main_stress);
+int orc_gauss_seidel(uint32_t N, const uint32_t *rp, const uint32_t *ci, const double *K,
+		     const double *b, double *x, uint32_t max_iter, double tol,
+		     uint32_t *niter, double *tol_reached);
+double orc_tension_damage(double E, double nu, double ft, double gf, const double *strain,
+			  double r_prev, double *r, double clfd);
+int orc_damage_solve(const orc_mesh_t *m, const orc_bcs_t *b, double E, double nu,
+		     double thickness, double density, int self_weight, const double gravity[2],
+		     double ft, double gf, uint32_t n_steps, uint32_t max_iter,
+		     uint32_t max_iter_noenh, double rtol, char *log, size_t cap,
+		     double *u_out, double *damage_out);
 void orc_simp_sensitivity(const orc_mesh_t *m, double nu, double thickness,
 			  const double *rho, double penal, double E0, double Emin,
 			  const double *a, const double *b, double *out);

@@ -73,6 +73,11 @@ def lib():
         L.orc_main_stress.restype = None
         L.orc_simp_sensitivity.argtypes = [vp, f64, f64, vp, f64, f64, f64, vp, vp, vp]
         L.orc_simp_sensitivity.restype = None
+        L.orc_gauss_seidel.argtypes = [u32, vp, vp, vp, vp, vp, u32, f64, vp, vp]
+        L.orc_tension_damage.argtypes = [f64, f64, f64, f64, vp, f64, vp, f64]
+        L.orc_tension_damage.restype = f64
+        L.orc_damage_solve.argtypes = [vp, vp, f64, f64, f64, f64, i32, vp, f64, f64, u32, u32,
+                                       u32, f64, C.c_char_p, C.c_size_t, vp, vp]
         L.orc_wtime.restype = f64
         L.orc_max_threads.restype = i32
         _lib = L
@@ -227,6 +232,34 @@ def fem(p, threads=1, tol=1e-8):
     out.update(u=u, cg_niter=it, cg_tol_reached=tr, cg_status=cst)
     out["strain"] = strain(fl, u)
     return out
+
+
+def gauss_seidel(rp, ci, K, b, x0=None, max_iter=None, tol=1e-8):
+    """nb_sparse_solve_Gauss_Seidel (gauss_seidel.c:14-58)."""
+    N = rp.shape[0] - 1
+    x = np.zeros(N) if x0 is None else np.array(x0, np.float64)
+    b = np.ascontiguousarray(b, np.float64)
+    it, tr = C.c_uint32(0), C.c_double(0)
+    st = lib().orc_gauss_seidel(N, _p(rp), _p(ci), _p(K), _p(b), _p(x),
+                                60 * N if max_iter is None else max_iter, tol,
+                                C.byref(it), C.byref(tr))
+    return x, int(it.value), float(tr.value), int(st)
+
+
+def damage(p, ft, gf, n_steps, max_iter, max_iter_noenh, rtol, log_cap=1 << 20):
+    """nbots' quasi-static damage solve (static_damage2D.c:239-470), CG path,
+    material E = p.E[0].  Returns (log text, displacements, damage per Gauss
+    point, number of Gauss-Seidel fallbacks)."""
+    fl = Flat(p)
+    ngp = 4 if p.conn.shape[1] == 4 else 1
+    u = np.zeros(p.n_dof)
+    d = np.zeros(ngp * p.n_elems)
+    buf = C.create_string_buffer(log_cap)
+    n_gs = lib().orc_damage_solve(C.byref(fl.mesh), C.byref(fl.bcs), float(p.E[0]), p.nu,
+                                  p.thickness, p.density, int(p.self_weight), _p(fl.grav), ft,
+                                  gf, n_steps, max_iter, max_iter_noenh, rtol, buf, log_cap,
+                                  _p(u), _p(d))
+    return buf.value.decode(), u, d, n_gs
 
 
 def wtime():

@@ -694,8 +694,63 @@ static int run_utest(const char *txt, uint32_t nvtx, const char *mesh_out,
 	return 0;
 }
 
+/* nbots' own nonlinear (damage) solve on a problem file
+ * (static_damage2D.c:239-470); its only output is the log, dumped as bytes.
+ * Material: E[0], nu of the problem, traction limit ft, fracture energy gf. */
+static int run_damage(const char *in, const char *out, double ft, double gf,
+		      uint32_t n_steps, uint32_t max_iter, uint32_t max_iter_noenh, double rtol)
+{
+	problem_t p;
+	read_problem(in, &p);
+	nb_mesh2D_t *part = xalloc(nb_mesh2D_get_memsize(p.nen == 4 ? NB_QUAD : NB_TRIAN));
+	void *msh;
+	build_mesh(&p, part, &msh);
+	nb_fem_elem_t *elem = nb_fem_elem_create(p.nen == 4 ? NB_QUAD_LINEAR : NB_TRG_LINEAR);
+	nb_bcond_t *bcond = xalloc(nb_bcond_get_memsize(2));
+	nb_bcond_init(bcond, 2);
+	build_bcond(&p, bcond);
+	nb_analysis2D_params params2D = {p.thickness, 0.0, 0};
+	nb_material_t *mat = nb_material_create();
+	nb_material_set_elasticity_module(mat, p.E[0]);
+	nb_material_set_poisson_module(mat, p.nu);
+	nb_material_set_density(mat, p.density);
+	nb_material_set_traction_limit_stress(mat, ft);
+	nb_material_set_fracture_energy(mat, gf);
+	nb_fem_implicit_t *ip = nb_fem_implicit_create();
+	nb_fem_implicit_set_N_steps(ip, n_steps);
+	nb_fem_implicit_set_N_max_iter(ip, max_iter);
+	nb_fem_implicit_set_N_max_iter_without_enhance(ip, max_iter_noenh);
+	nb_fem_implicit_set_residual_tolerance(ip, rtol);
+	char logpath[4096];
+	snprintf(logpath, sizeof(logpath), "%s.log", out);
+	remove(logpath);
+	double grav[2] = {p.gravity[0], p.gravity[1]};
+	nb_fem_compute_2D_Non_Linear_Solid_Mechanics(part, elem, mat, bcond, p.self_weight != 0,
+						     grav, false, NB_PLANE_STRESS, &params2D, ip,
+						     logpath);
+	FILE *lf = fopen(logpath, "rb");
+	if (!lf) { perror(logpath); return 2; }
+	fseek(lf, 0, SEEK_END);
+	long n = ftell(lf);
+	fseek(lf, 0, SEEK_SET);
+	char *txt = xalloc((size_t)n + 1);
+	if (fread(txt, 1, (size_t)n, lf) != (size_t)n) { fprintf(stderr, "short log\n"); return 2; }
+	fclose(lf);
+	g_out = fopen(out, "wb");
+	if (!g_out) { perror(out); return 2; }
+	dump("damage_log", DT_U8, txt, (uint64_t)n);
+	fclose(g_out);
+	nb_fem_implicit_destroy(ip);
+	nb_material_destroy(mat);
+	return 0;
+}
+
 int main(int argc, char **argv)
 {
+	if (argc >= 10 && !strcmp(argv[1], "damage"))
+		return run_damage(argv[2], argv[3], atof(argv[4]), atof(argv[5]),
+				  (uint32_t)atoi(argv[6]), (uint32_t)atoi(argv[7]),
+				  (uint32_t)atoi(argv[8]), atof(argv[9]));
 	if (argc >= 4 && !strcmp(argv[1], "problem"))
 		return run_problem(argv[2], argv[3], argc > 4 ? (uint32_t)atoi(argv[4]) : 1);
 	if (argc >= 6 && !strcmp(argv[1], "utest"))

@@ -72,6 +72,30 @@ def small_cases():
     return cases
 
 
+# nbots' damage solve (static_damage2D.c:239-470): name -> (problem source,
+# ft, gf, N_steps, N_max_iter, N_max_iter_without_enhance, residual tol)
+DAMAGE_CASES = {
+    # converges in every step; no Gauss-Seidel fallback
+    "dmg_q4_16x8": ("q4", 6.0, 10.0, 4, 40, 6, 1e-7),
+    # every conjugate-gradient solve fails and falls back to Gauss-Seidel,
+    # which fails too (the absolute tolerance 1e-8 is out of reach)
+    "dmg_t3_beam150": ("beam150", 1e4, 10.0, 2, 30, 5, 1e-6),
+}
+
+
+def damage_problem(src, tmp, a):
+    if src == "q4":
+        p = W.cantilever_q4(16, 8, point_load=-0.5, name="dmg_q4_16x8")
+        path = os.path.join(tmp, "dmg_q4.bin")
+        P.write_problem(p, path)
+        return path
+    inputs = os.path.join(a.nbots_src, "utest/sources/nb/pde_bot/static_elasticity2D_inputs")
+    path = os.path.join(tmp, "beam150.bin")
+    run([HARNESS, "utest", os.path.join(inputs, "beam_cantilever.txt"), "150", path,
+         os.path.join(tmp, "beam150.fem")])
+    return path
+
+
 def run(cmd):
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode:
@@ -88,11 +112,15 @@ def save(name, prob_path, dump):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--nbots-src", default="/root/reference")
+    ap.add_argument("--only", nargs="*", help="regenerate these cases only")
     a = ap.parse_args()
+    want = (lambda name: True) if not a.only else (lambda name: name in a.only)
     run(["make", "-s", "-C", ROOT, "-f", "oracle/Makefile.ref", f"NBOTS_SRC={a.nbots_src}",
          "-j8", "harness"])
     tmp = tempfile.mkdtemp()
     for name, p in small_cases().items():
+        if not want(name):
+            continue
         pb = os.path.join(tmp, name + ".bin")
         ob = os.path.join(tmp, name + ".out")
         P.write_problem(p, pb)
@@ -101,6 +129,8 @@ def main():
     inputs = os.path.join(a.nbots_src, "utest/sources/nb/pde_bot/static_elasticity2D_inputs")
     for name, txt, extra in [("t3_beam_cantilever", "beam_cantilever.txt", []),
                              ("t3_plate_with_hole", "plate_with_hole.txt", ["pwh"])]:
+        if not want(name):
+            continue
         mb = os.path.join(tmp, name + ".bin")
         ob = os.path.join(tmp, name + ".fem")
         run([HARNESS, "utest", os.path.join(inputs, txt), "1000", mb, ob] + extra)
@@ -111,6 +141,16 @@ def main():
         d = P.read_dump(ob2)
         d.update({k: v for k, v in fem.items()})
         save(name, mb, d)
+    for name, (src, ft, gf, steps, mi, mne, rtol) in DAMAGE_CASES.items():
+        if not want(name):
+            continue
+        pb = damage_problem(src, tmp, a)
+        ob = os.path.join(tmp, name + ".out")
+        run([HARNESS, "damage", pb, ob, repr(ft), repr(gf), str(steps), str(mi), str(mne),
+             repr(rtol)])
+        d = P.read_dump(ob)
+        d["damage_params"] = np.array([ft, gf, steps, mi, mne, rtol], np.float64)
+        save(name, pb, d)
 
 
 if __name__ == "__main__":
