@@ -187,9 +187,13 @@ int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, doub
 				logf_append(lf, "    [%i: Residual: %e ]\n", (int)iter, residual_norm);
 				break;
 			}
+			/* returns 1 (and cg.status 1) when the tolerance is not reached */
 			nbg_cg_result_t cg;
-			TRY(nbg_cg_f64(N, f->row_ptr, f->col_idx, f->K, w.res, w.du, N, 1e-8,
-				       NBG_CG_JACOBI, &cg, f->cg_ws, f->cg_ws_bytes, f->stream));
+			const int st = nbg_cg_f64(N, f->row_ptr, f->col_idx, f->K, w.res, w.du, N,
+						  1e-8, NBG_CG_JACOBI, &cg, f->cg_ws,
+						  f->cg_ws_bytes, f->stream);
+			if (st < 0)
+				TRY(st);
 			if (cg.status < 0)
 				TRY(cg.status);
 			inf.cg_solves++;

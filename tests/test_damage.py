@@ -9,8 +9,8 @@ GPU: Gauss-Seidel on the device repeats nbots' sweeps bit for bit (the
 sweep's per-row arithmetic is nbots'; only the error sum is ordered
 differently); the device damage loop, through the C ABI and through the
 drop-in symbol, takes the same iterations per load step as nbots and its
-residuals, displacements and damage agree with the oracle's to 1e-6
-relative.  The conjugate-gradient solves inside are the device CG, whose
+residuals agree with nbots' to 1e-6 relative plus the inner solves'
+absolute tolerance 1e-8, displacements and damage with the oracle's to 1e-6.  The conjugate-gradient solves inside are the device CG, whose
 sums run in another order than nbots', so the run is not bit-exact.
 """
 import ctypes as C
@@ -167,7 +167,9 @@ def check_q4_run(log, u, dmg, p, d):
     for (k, a), (_, b) in zip(got, ref):
         if k == "res":
             assert a[0] == b[0] and a[2] == b[2]
-            assert abs(a[1] - b[1]) <= 1e-6 * max(abs(b[1]), 1e-6), (a, b)
+            # the inner solves stop at an absolute residual of 1e-8, and
+            # their last digits follow their summation order
+            assert abs(a[1] - b[1]) <= 1e-6 * abs(b[1]) + 1e-8, (a, b)
     _, uo, do, _ = O.damage(p, *params(d))
     assert np.linalg.norm(u - uo) <= 1e-6 * np.linalg.norm(uo)
     assert np.max(np.abs(dmg - do)) <= 1e-6
@@ -204,19 +206,20 @@ def test_gpu_damage_dropin(tmp_path):
 
 @pytest.mark.gpu
 def test_gpu_damage_gauss_seidel_fallback(tmp_path):
-    """Every solve of this run falls back to Gauss-Seidel, which fails: the
-    device run logs the same failure records with nbots' sweep count 60 N,
-    and its first residual (the load itself) agrees with nbots'."""
+    """From the second iteration on, the solves of this run fall back to
+    Gauss-Seidel, which fails: the device run logs the same records in the
+    same order, with nbots' sweep count 60 N, and its first residual (the
+    load itself) agrees with nbots'."""
     from nbots_gb300.fem import FemSystem
     p, d = load_golden("dmg_t3_beam150")
     s = FemSystem(p)
     logf = tmp_path / "gs.log"
     ft, gf, steps, mi, mne, rtol = params(d)
-    info = s.damage(ft, gf, steps, 1, mne, rtol, logfile=logf)
+    info = s.damage(ft, gf, steps, 2, mne, rtol, logfile=logf)
     got = parse(logf.read_text())
     ref = parse(bytes(d["damage_log"]).decode())
     assert info.gs_fallbacks >= 1 and info.gs_failures == info.gs_fallbacks
-    assert [k for k, _ in got[:6]] == [k for k, _ in ref[:6]]
+    assert [k for k, _ in got[:7]] == [k for k, _ in ref[:7]]
     assert got[2][1][1] == pytest.approx(ref[2][1][1], rel=1e-6)
     assert got[4][1][0] == ref[4][1][0] == 60 * p.n_dof
     s.close()
