@@ -183,6 +183,56 @@ def bench_c4(lib, L, W):
     return out
 
 
+def _damage_step_iters(log):
+    """Residual evaluations per load step of an nbots damage log."""
+    out = []
+    for line in log.splitlines():
+        if "Load step" in line:
+            out.append(0)
+        elif "Residual" in line:
+            out[-1] += 1
+    return out
+
+
+def bench_damage(L, W, with_cpu):
+    """nbots' quasi-static damage solve (static_damage2D.c:239-470) on a
+    cantilever under a uniform top traction: 4 load steps, at most 40
+    iterations each, 6 without a new best residual, residual tolerance
+    1e-7, ft = 6, Gf = 10, E = 1.  Wall time of nbg_fem_damage (device
+    assembly with damage, boundary conditions, residual, nbots-order Jacobi
+    PCG, strain and damage, host log) against the oracle's one-thread
+    restatement of nbots' loop on the same problem."""
+    import tempfile
+    from nbots_gb300.fem import FemSystem
+    out = {}
+    args_ = (6.0, 10.0, 4, 40, 6, 1e-7)
+    for nx, ny, cpu in ((128, 64, with_cpu), (512, 256, False)):
+        p = W.cantilever_q4(nx, ny, point_load=0.0, top_traction=0.35)
+        s = FemSystem(p)
+        with tempfile.TemporaryDirectory() as td:
+            logf = os.path.join(td, "dmg.log")
+            s.damage(*args_, logfile=None)  # warm (module load, workspaces)
+            t0 = time.perf_counter()
+            info = s.damage(*args_, logfile=logf)
+            t_gpu = time.perf_counter() - t0
+            log = open(logf).read()
+        s.close()
+        row = {"workload": f"Q4 cantilever {nx}x{ny}, {p.n_dof} dof, top traction 0.35",
+               "gpu_s": t_gpu, "iterations": info.iterations, "cg_solves": info.cg_solves,
+               "cg_iterations": info.cg_iterations, "gs_fallbacks": info.gs_fallbacks,
+               "step_iterations": _damage_step_iters(log)}
+        if cpu:
+            from oracle import oracle as O
+            t0 = time.perf_counter()
+            olog, _, _, _ = O.damage(p, *args_)
+            t_cpu = time.perf_counter() - t0
+            row.update(cpu_oracle_s=t_cpu, cpu_cores=1,
+                       cpu_step_iterations=_damage_step_iters(olog),
+                       speedup=t_cpu / t_gpu)
+        out[f"{nx}x{ny}"] = row
+    return out
+
+
 def bench_c5(args, lib, L, W, sp, dev, stream, flush):
     """96 batched SIMP cantilevers: one graph launch = zero u, batched mixed
     CG to relres 1e-8 per instance, compliance sensitivities.  Per-instance
@@ -622,6 +672,7 @@ def run_gpu(args):
 
     c4 = None if args.no_c4 else bench_c4(lib, L, W)
     c5 = None if args.no_c5 else bench_c5(args, lib, L, W, sp, dev, stream, flush)
+    dmg = None if args.no_damage else bench_damage(L, W, rank == 0 and not args.no_cpu_baseline)
 
     cpu = None
     if rank == 0 and not args.no_cpu_baseline:
@@ -664,6 +715,7 @@ def run_gpu(args):
                             "(mixed) from pinned host buffers"},
             "c4_simp": c4,
             "c5_batch": c5,
+            "damage": dmg,
             "cpu_baseline": cpu,
             "gpu_launches": args.steps,
             "dof_iters_per_s": N * it / t_all,
@@ -740,6 +792,7 @@ def main():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-c4", action="store_true", help="skip the SIMP gradient timings")
     ap.add_argument("--no-c5", action="store_true", help="skip the batched solves")
+    ap.add_argument("--no-damage", action="store_true", help="skip the damage-solve timings")
     ap.add_argument("--c3", action="store_true",
                     help="run the 4M-dof unstructured T3 L-shape instead (mesh generation "
                          "takes about a minute on the host)")

@@ -11,9 +11,14 @@
 // bound the iteration: folding L3 into the next SpMV (recomputing -q + beta p
 // for every gathered column) saves a barrier but costs five per nonzero; on
 // the 1M-dof cantilever the folded form took 1.58 s for 7,017 iterations,
-// this one 1.11 s.  The scalar recurrences run in thread 0;
-// the dot products are summed by warp 0 in a fixed order, identical from run
-// to run.
+// this one 1.11 s.  The SpMV of L1 is warp-staged (warp_rows_exact): a warp
+// loads the values and columns of 32 rows with coalesced loads, gathers p for
+// all their products at once, then each lane adds its own row's products in
+// nbots' order; with one row per thread this took the 16,770-dof cantilever
+// from 43 to 21 us per iteration (a thread walking its row alone waits on
+// each dependent column load in turn).  The scalar recurrences run in thread
+// 0; the dot products are summed by warp 0 in a fixed order, identical from
+// run to run.
 #include <cstdint>
 #include <cstdio>
 #include <mutex>
@@ -25,6 +30,7 @@ using namespace nbg;
 namespace {
 
 constexpr int kThreads = 256;
+constexpr int kStage = 576;  // products staged per warp and pass: 32 rows of 18
 
 struct CgDevResult {
     uint32_t niter;
@@ -60,6 +66,8 @@ struct CgArgs {
 template <bool JAC>
 __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
     __shared__ double buf[3 * kThreads];
+    __shared__ double prod[kThreads / 32][kStage];  // staged products of A p
+    const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ double s_coef;  // alpha, then beta
     __shared__ int s_stop;
     __shared__ struct {
@@ -120,14 +128,18 @@ __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
     while (!s_stop) {
         {   // L1: w = A p; p.w, g.g (the lagged norm nbots tests), g.q
             double v3[3] = {0.0, 0.0, 0.0};
-            for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
-                double s = 0.0;
-                for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++) s = add(s, mul(val[kk], p[ci[kk]]));
-                a.w[r] = s;
-                const double gi = a.g[r], qi = a.q[r];
-                v3[0] = add(v3[0], mul(p[r], s));
-                v3[1] = add(v3[1], mul(gi, gi));
-                v3[2] = add(v3[2], mul(gi, qi));
+            for (uint32_t g0 = r0 + warp * 32; g0 < r1; g0 += kThreads) {
+                const uint32_t nrows = min(32u, r1 - g0);
+                const double s = warp_rows_exact<kStage>(rp, ci, val, p, g0, nrows,
+                                                         prod[warp], lane);
+                if ((uint32_t)lane < nrows) {
+                    const uint32_t r = g0 + lane;
+                    a.w[r] = s;
+                    const double gi = a.g[r], qi = a.q[r];
+                    v3[0] = add(v3[0], mul(p[r], s));
+                    v3[1] = add(v3[1], mul(gi, gi));
+                    v3[2] = add(v3[2], mul(gi, qi));
+                }
             }
             double t[3];
             block_sum_f64<3>(v3, buf, t);
@@ -270,7 +282,7 @@ extern "C" int nbg_cg_f64(uint32_t N, const uint32_t* row_ptr, const uint32_t* c
     CgDevResult hr{};
     if (e == cudaSuccess) {
         unsigned G = (unsigned)(nsm * (occ < 2 ? occ : 2));
-        const unsigned want = (N + kThreads * 4 - 1) / (kThreads * 4);
+        const unsigned want = (N + kThreads - 1) / kThreads;
         if (want < G) G = want;
         if (G < 1) G = 1;
         if (G > kMaxBlocks) G = kMaxBlocks;

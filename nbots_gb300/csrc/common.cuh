@@ -293,4 +293,37 @@ __device__ __forceinline__ FF ff_mul(FF a, FF b) {
     return fast_two_sum(p.hi, e);
 }
 
+// Rows row0 .. row0 + nrows - 1 (nrows <= 32) of a CSR matrix times x in
+// nbots' order (each row starts at 0 and adds its rounded products left to
+// right, sparse.c:405-414), so the sums are bit-exact.  The warp stages the
+// products of all its rows through `prod` (kStage doubles of this warp's
+// shared memory) with coalesced loads of values and columns and independent
+// gathers of x; then each lane adds its own row's products in column order
+// and gets its row's sum (0 for lanes >= nrows).  All 32 lanes must call it.
+template <int kStage>
+__device__ __forceinline__ double warp_rows_exact(const uint32_t* __restrict__ rp,
+                                                  const uint32_t* __restrict__ ci,
+                                                  const double* __restrict__ v,
+                                                  const double* x, uint32_t row0,
+                                                  uint32_t nrows, double* prod, int lane) {
+    const uint32_t k0 = rp[row0], k1 = rp[row0 + nrows];
+    uint32_t mb = 0, me = 0;
+    if ((uint32_t)lane < nrows) {
+        mb = rp[row0 + lane];
+        me = rp[row0 + lane + 1];
+    }
+    double s = 0.0;
+    uint32_t next = mb;  // next product of this lane's row still to add
+    for (uint32_t base = k0; base < k1; base += kStage) {
+        const uint32_t cnt = min((uint32_t)kStage, k1 - base);
+#pragma unroll 4
+        for (uint32_t t = lane; t < cnt; t += 32) prod[t] = mul(v[base + t], x[ci[base + t]]);
+        __syncwarp();
+        const uint32_t hi = min(me, base + cnt);
+        for (; next < hi; next++) s = add(s, prod[next - base]);
+        __syncwarp();
+    }
+    return s;
+}
+
 }  // namespace nbg

@@ -27,23 +27,8 @@ __global__ void __launch_bounds__(kWarps * 32) k_spmv_csr_exact(uint32_t N,
     const uint32_t row0 = (blockIdx.x * kWarps + warp) * 32u;
     if (row0 >= N) return;
     const uint32_t nrows = min(32u, N - row0);
-    const uint32_t k0 = rp[row0], k1 = rp[row0 + nrows];
     const uint32_t my_row = row0 + lane;
-    uint32_t mb = 0, me = 0;
-    if (lane < nrows) {
-        mb = rp[my_row];
-        me = rp[my_row + 1];
-    }
-    double s = 0.0;
-    uint32_t next = mb;  // next product of my row still to add
-    for (uint32_t base = k0; base < k1; base += kStage) {
-        const uint32_t cnt = min((uint32_t)kStage, k1 - base);
-        for (uint32_t t = lane; t < cnt; t += 32) prod[warp][t] = mul(v[base + t], x[ci[base + t]]);
-        __syncwarp();
-        const uint32_t hi = min(me, base + cnt);
-        for (; next < hi; next++) s = add(s, prod[warp][next - base]);
-        __syncwarp();
-    }
+    const double s = warp_rows_exact<kStage>(rp, ci, v, x, row0, nrows, prod[warp], lane);
     if (lane < nrows) y[my_row] = s;
 }
 

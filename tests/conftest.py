@@ -19,6 +19,17 @@ def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300, sm_103a)")
 
 
+def cg_iters_close(it, ref_it, bnorm, tol=1e-8):
+    """nbots' CG stops on an absolute tolerance.  Where that is far below the
+    rounding level of the residual (tol < 1e-14 ||b||, the T3 beam with
+    E = 2e11), the stop point follows the summation order of the dot
+    products and only the displacements carry the contract: the count must
+    stay within a factor 1.5.  Elsewhere it stays within 10%."""
+    if tol < 1e-14 * bnorm:
+        return ref_it / 1.5 <= it <= ref_it * 1.5
+    return abs(it - ref_it) <= max(2, ref_it // 10)
+
+
 def load_golden(name):
     """(Problem, dict of reference dumps) for one committed fixture."""
     from nbots_gb300 import problem_io as P

@@ -7,7 +7,7 @@ import ctypes as C
 import numpy as np
 import pytest
 
-from conftest import GOLDEN_CASES, load_golden
+from conftest import GOLDEN_CASES, cg_iters_close, load_golden
 from kat import BEAM_MAX_DISP, PWH_MAX_VM_ERR, max_disp, pwh_mean_vm_error
 
 pytestmark = pytest.mark.gpu
@@ -56,11 +56,7 @@ def test_fem_stages_vs_reference(lib, name):
     r = s.solve()
     u = s.get(L.FEM_U)
     assert r.status == int(d["cg_status"][0])
-    # nbots' stop is absolute (1e-8); when that is below the rounding level of
-    # the residual (the T3 beam: E = 2e11) the stop point depends on the
-    # summation order, so only the displacements carry the contract
-    ref_it = int(d["cg_niter"][0])
-    assert abs(r.niter - ref_it) <= max(2, ref_it // 10)
+    assert cg_iters_close(r.niter, int(d["cg_niter"][0]), np.linalg.norm(d["F_bc"]))
     assert rel(u, d["u"]) < U_REL_TOL
     # strain of the reference displacements is bit-exact
     s.put(L.FEM_U, d["u"])
