@@ -380,6 +380,19 @@ typedef struct {
  * row_ptr is filled (its last entry is nnz). */
 int nbg_host_pattern(const nbg_mesh_t *m, uint32_t *row_ptr, uint32_t *col_idx);
 
+/* The same three structures built on the device from device copies of the
+ * connectivity and edges (pattern.cu): row_ptr[2 N_nod + 1], the incidence
+ * (inc_ptr[N_nod + 1], inc_elem and inc_local [nen N_elem]) and, when
+ * slice_off is not NULL, the block plan slice_off[ceil(N_nod / 32) + 1].
+ * col_idx is allocated here (nbg_dev_alloc-compatible; free it with
+ * nbg_dev_free) and *nnz set.  Word for word equal to nbg_host_pattern,
+ * nbg_host_incidence and nbg_bsr_plan.  A node index out of range returns
+ * NBG_ERR_ARG before anything is written. */
+int nbg_pattern_dev(uint32_t nen, uint32_t N_nod, uint32_t N_elem, uint32_t N_edg,
+                    const uint32_t *conn, const uint32_t *edg, uint32_t *row_ptr,
+                    uint32_t **col_idx, uint64_t *nnz, uint32_t *inc_ptr, uint32_t *inc_elem,
+                    uint8_t *inc_local, uint32_t *slice_off, void *stream);
+
 /* Node -> (element, local node) incidence in ascending element order. */
 int nbg_host_incidence(const nbg_mesh_t *m, uint32_t *inc_ptr, uint32_t *inc_elem,
                        uint8_t *inc_local);

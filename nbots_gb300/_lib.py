@@ -140,6 +140,8 @@ SIGS = {
                       C.POINTER(SimpInfo)], i32),
     "nbg_host_pattern": ([vp, vp, vp], i32),
     "nbg_host_incidence": ([vp, vp, vp, vp], i32),
+    "nbg_pattern_dev": ([u32, u32, u32, u32, vp, vp, vp, C.POINTER(vp), C.POINTER(u64), vp, vp,
+                         vp, vp, vp], i32),
     "nbg_fem_create": ([C.POINTER(vp), vp, vp], i32),
     "nbg_fem_destroy": ([vp], None),
     "nbg_fem_n_dof": ([vp], u32),

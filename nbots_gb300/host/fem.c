@@ -261,8 +261,6 @@ void nbg_fem_destroy(nbg_fem_t *f)
 int nbg_fem_create(nbg_fem_t **out, const nbg_mesh_t *m, void *stream)
 {
 	int rc = NBG_OK;
-	uint32_t *rp = NULL, *ci = NULL, *ip = NULL, *ie = NULL;
-	uint8_t *il = NULL;
 	*out = NULL;
 	if (!m || (m->nen != 3 && m->nen != 4) || m->N_nod == 0)
 		return NBG_ERR_ARG;
@@ -276,29 +274,15 @@ int nbg_fem_create(nbg_fem_t **out, const nbg_mesh_t *m, void *stream)
 	f->stream = stream;
 	f->N = 2 * m->N_nod;
 	const size_t ne = m->N_elem, nen = m->nen, Nn = m->N_nod;
-	rp = malloc(((size_t)f->N + 1) * sizeof(uint32_t));
-	ip = malloc((Nn + 1) * sizeof(uint32_t));
-	ie = malloc((ne * nen + 1) * sizeof(uint32_t));
-	il = malloc(ne * nen + 1);
-	if (!rp || !ip || !ie || !il)
-		TRY(NBG_ERR_NOMEM);
-	TRY(nbg_host_pattern(m, rp, NULL));
-	f->nnz = rp[f->N];
-	ci = malloc((f->nnz + 1) * sizeof(uint32_t));
-	if (!ci)
-		TRY(NBG_ERR_NOMEM);
-	TRY(nbg_host_pattern(m, rp, ci));
-	TRY(nbg_host_incidence(m, ip, ie, il));
-
 	const size_t nd = 2 * nen;
+	const uint32_t S = (m->N_nod + 31) / 32;
+	void *edg_d = NULL;
 	TRY(nbg_dev_alloc((void **)&f->nod, 16 * Nn));
 	TRY(nbg_dev_alloc((void **)&f->conn, 4 * ne * nen));
 	TRY(nbg_dev_alloc((void **)&f->row_ptr, 4 * ((size_t)f->N + 1)));
-	TRY(nbg_dev_alloc((void **)&f->col_idx, 4 * f->nnz));
 	TRY(nbg_dev_alloc((void **)&f->inc_ptr, 4 * (Nn + 1)));
 	TRY(nbg_dev_alloc((void **)&f->inc_elem, 4 * ne * nen));
 	TRY(nbg_dev_alloc((void **)&f->inc_local, ne * nen));
-	TRY(nbg_dev_alloc((void **)&f->K, 8 * f->nnz));
 	TRY(nbg_dev_alloc((void **)&f->F, 8 * (size_t)f->N));
 	TRY(nbg_dev_alloc((void **)&f->u, 8 * (size_t)f->N));
 	TRY(nbg_dev_alloc((void **)&f->E, 8 * ne));
@@ -308,47 +292,40 @@ int nbg_fem_create(nbg_fem_t **out, const nbg_mesh_t *m, void *stream)
 	TRY(nbg_dev_alloc((void **)&f->distorted, 256));
 	TRY(nbg_dev_alloc((void **)&f->matched, 256));
 	TRY(nbg_dev_alloc((void **)&f->status, 256));
+	TRY(nbg_dev_alloc((void **)&f->slice_off, 4 * ((size_t)S + 1)));
+	TRY(nbg_dev_alloc(&edg_d, 8 * (size_t)(m->N_edg ? m->N_edg : 1)));
 	TRY(nbg_h2d(f->nod, m->nod, 16 * Nn, stream));
 	TRY(nbg_h2d(f->conn, m->conn, 4 * ne * nen, stream));
-	TRY(nbg_h2d(f->row_ptr, rp, 4 * ((size_t)f->N + 1), stream));
-	TRY(nbg_h2d(f->col_idx, ci, 4 * f->nnz, stream));
-	TRY(nbg_h2d(f->inc_ptr, ip, 4 * (Nn + 1), stream));
-	TRY(nbg_h2d(f->inc_elem, ie, 4 * ne * nen, stream));
-	TRY(nbg_h2d(f->inc_local, il, ne * nen, stream));
+	TRY(nbg_h2d(edg_d, m->edg, 8 * (size_t)m->N_edg, stream));
+	/* pattern, incidence and block plan, built on the device (pattern.cu) */
+	TRY(nbg_pattern_dev(m->nen, m->N_nod, m->N_elem, m->N_edg, f->conn, edg_d, f->row_ptr,
+			    &f->col_idx, &f->nnz, f->inc_ptr, f->inc_elem, f->inc_local,
+			    f->slice_off, stream));
+	nbg_dev_free(edg_d);
+	edg_d = NULL;
+	TRY(nbg_dev_alloc((void **)&f->K, 8 * f->nnz));
 	{
-		/* block layout plan of the fixed pattern */
-		uint32_t S = (m->N_nod + 31) / 32;
-		uint32_t *so = malloc(((size_t)S + 1) * sizeof(uint32_t));
-		if (!so)
-			TRY(NBG_ERR_NOMEM);
-		if (nbg_bsr_plan(f->N, rp, ci, so) == NBG_OK) {
-			uint64_t ent = 32ull * so[S];
-			int r2 = nbg_dev_alloc((void **)&f->slice_off, 4 * ((size_t)S + 1));
-			if (r2 == NBG_OK)
-				r2 = nbg_h2d(f->slice_off, so, 4 * ((size_t)S + 1), stream);
-			if (r2 == NBG_OK)
-				r2 = nbg_dev_alloc((void **)&f->bcol, 4 * ent);
-			if (r2 != NBG_OK) {
-				free(so);
-				TRY(r2);
-			}
-			f->bsr.N = f->N;
-			f->bsr.Nn = m->N_nod;
-			f->bsr.n_slices = S;
-			f->bsr.n_entries = ent;
-			f->bsr.slice_off = f->slice_off;
-			f->bsr.bcol = f->bcol;
-			f->bsr_ok = 1;
-		}
-		free(so);
+		/* block layout of the fixed pattern: every node row pairs its two
+		 * dof rows by construction, so the plan always applies */
+		uint32_t wS = 0;
+		TRY(nbg_d2h(&wS, f->slice_off + S, 4, stream));
+		TRY(nbg_stream_sync(stream));
+		const uint64_t ent = 32ull * wS;
+		TRY(nbg_dev_alloc((void **)&f->bcol, 4 * ent));
+		f->bsr.N = f->N;
+		f->bsr.Nn = m->N_nod;
+		f->bsr.n_slices = S;
+		f->bsr.n_entries = ent;
+		f->bsr.slice_off = f->slice_off;
+		f->bsr.bcol = f->bcol;
+		f->bsr_ok = 1;
 	}
 	TRY(nbg_stream_sync(stream));
 	(void)nd;
-	free(rp); free(ci); free(ip); free(ie); free(il);
 	*out = f;
 	return NBG_OK;
 fail:
-	free(rp); free(ci); free(ip); free(ie); free(il);
+	nbg_dev_free(edg_d);
 	nbg_fem_destroy(f);
 	return rc;
 }
