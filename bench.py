@@ -720,6 +720,10 @@ def run_gpu(args):
                          "bound": "fp64 issue (about 2 FP64 FMA per clock per SM on GB300)"},
             "nbots_order_fp64_gpu": {"s_per_solve": float(t_exact[0]), "iters": r_exact.niter},
             "speedup_mixed_vs_fp64_gpu": float(np.median(t_fp64)) / t_all,
+            "speedup_mixed_vs_plain_fp64_gpu": float(t_exact[0]) / t_all,
+            "speedup_note": "plain = the FP64 GPU path that matches nbots (CSR, nbots' "
+                            "arithmetic and iteration, the drop-in's solver); fp64 = the "
+                            "tuned FP64 block-layout CG",
             "setup_s": {"pattern_and_upload": t_create, "first_call": t_create_first,
                         "host_pattern_and_incidence": t_host_pattern,
                         "assembly_and_bcs": t_asm},
@@ -760,7 +764,24 @@ def run_profile(args):
     from nbots_gb300 import workloads as W
     from nbots_gb300.fem import FemSystem
     lib = L.lib()
+    if args.profile == "damage":
+        # the damage solve of the bench's 128x64 case, once
+        p = W.cantilever_q4(128, 64, point_load=0.0, top_traction=0.35)
+        s = FemSystem(p)
+        info = s.damage(6.0, 10.0, 4, 40, 6, 1e-7)
+        print(json.dumps({"profile": "damage", "dof": s.N, "iterations": info.iterations,
+                          "cg_iterations": info.cg_iterations}))
+        s.close()
+        return 0
     p = W.config_c2()
+    if args.profile == "pattern":
+        # pattern, incidence and block plan of the 1M-dof mesh, twice
+        for _ in range(2):
+            s = FemSystem(p)
+            n = s.nnz
+            s.close()
+        print(json.dumps({"profile": "pattern", "nodes": p.n_nodes, "nnz": n}))
+        return 0
     s = FemSystem(p)
     assert s.assemble() == 0
     s.apply_bcs()
@@ -819,7 +840,7 @@ def main():
     ap.add_argument("--c3", action="store_true",
                     help="run the 4M-dof unstructured T3 L-shape instead (mesh generation "
                          "takes about a minute on the host)")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "spmv"],
+    ap.add_argument("--profile", choices=["mixed", "fp64", "spmv", "damage", "pattern"],
                     help="one bounded kernel launch for ncu instead of the benchmark")
     ap.add_argument("--iters", type=int, default=100)
     args = ap.parse_args()

@@ -16,7 +16,10 @@
 // all their products at once, then each lane adds its own row's products in
 // nbots' order; with one row per thread this took the 16,770-dof cantilever
 // from 43 to 21 us per iteration (a thread walking its row alone waits on
-// each dependent column load in turn).  The scalar recurrences run in thread
+// each dependent column load in turn).  It is used up to two rows per thread
+// of the grid; on the 1M-dof cantilever (14 rows per thread) it took 230 us
+// per iteration against 158 for the plain thread-per-row loop, which keeps
+// the FP64 pipe fed from many independent rows.  The scalar recurrences run in thread
 // 0; the dot products are summed by warp 0 in a fixed order, identical from
 // run to run.
 #include <cstdint>
@@ -63,10 +66,10 @@ struct CgArgs {
     unsigned flags;
 };
 
-template <bool JAC>
+template <bool JAC, bool STAGED>
 __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
     __shared__ double buf[3 * kThreads];
-    __shared__ double prod[kThreads / 32][kStage];  // staged products of A p
+    __shared__ double prod[STAGED ? kThreads / 32 : 1][STAGED ? kStage : 1];
     const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
     __shared__ double s_coef;  // alpha, then beta
     __shared__ int s_stop;
@@ -128,12 +131,25 @@ __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
     while (!s_stop) {
         {   // L1: w = A p; p.w, g.g (the lagged norm nbots tests), g.q
             double v3[3] = {0.0, 0.0, 0.0};
-            for (uint32_t g0 = r0 + warp * 32; g0 < r1; g0 += kThreads) {
-                const uint32_t nrows = min(32u, r1 - g0);
-                const double s = warp_rows_exact<kStage>(rp, ci, val, p, g0, nrows,
-                                                         prod[warp], lane);
-                if ((uint32_t)lane < nrows) {
-                    const uint32_t r = g0 + lane;
+            if constexpr (STAGED) {
+                for (uint32_t g0 = r0 + warp * 32; g0 < r1; g0 += kThreads) {
+                    const uint32_t nrows = min(32u, r1 - g0);
+                    const double s = warp_rows_exact<kStage>(rp, ci, val, p, g0, nrows,
+                                                             prod[warp], lane);
+                    if ((uint32_t)lane < nrows) {
+                        const uint32_t r = g0 + lane;
+                        a.w[r] = s;
+                        const double gi = a.g[r], qi = a.q[r];
+                        v3[0] = add(v3[0], mul(p[r], s));
+                        v3[1] = add(v3[1], mul(gi, gi));
+                        v3[2] = add(v3[2], mul(gi, qi));
+                    }
+                }
+            } else {
+                for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+                    double s = 0.0;
+                    for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++)
+                        s = add(s, mul(val[kk], p[ci[kk]]));
                     a.w[r] = s;
                     const double gi = a.g[r], qi = a.q[r];
                     v3[0] = add(v3[0], mul(p[r], s));
@@ -275,14 +291,22 @@ extern "C" int nbg_cg_f64(uint32_t N, const uint32_t* row_ptr, const uint32_t* c
     int rc = NBG_OK;
     cudaError_t e = cudaMemsetAsync(base + L.bar, 0, 3 * 256, s);
     int dev = 0, nsm = 0, occ = 0;
-    const void* fn = (flags & NBG_CG_JACOBI) ? (const void*)k_cg_f64<true> : (const void*)k_cg_f64<false>;
     if (e == cudaSuccess) e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    // at most two rows per thread of the grid: warp-staged SpMV (latency);
+    // more: one row per thread, the FP64 pipe busy with many rows in flight
+    const bool staged = (uint64_t)N <= 2ull * 2 * (uint64_t)nsm * kThreads;
+    const bool jac = (flags & NBG_CG_JACOBI) != 0;
+    const void* fn = jac ? (staged ? (const void*)k_cg_f64<true, true>
+                                   : (const void*)k_cg_f64<true, false>)
+                         : (staged ? (const void*)k_cg_f64<false, true>
+                                   : (const void*)k_cg_f64<false, false>);
     if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, fn, kThreads, 0);
     CgDevResult hr{};
     if (e == cudaSuccess) {
         unsigned G = (unsigned)(nsm * (occ < 2 ? occ : 2));
-        const unsigned want = (N + kThreads - 1) / kThreads;
+        const unsigned want = staged ? (N + kThreads - 1) / kThreads
+                                     : (N + kThreads * 4 - 1) / (kThreads * 4);
         if (want < G) G = want;
         if (G < 1) G = 1;
         if (G > kMaxBlocks) G = kMaxBlocks;
