@@ -387,6 +387,37 @@ def run_c3(args):
     t_mixed, r_mixed = min(tm, key=lambda x: x[0])
     t_fp64, r_fp64 = min(tf, key=lambda x: x[0])
     nblk = nnz // 4
+    # the same solves on a block layout in SELL-C-sigma node order (sigma 512)
+    m = FemSystem(p, stream=sp)
+    m.set_block_order(L.ORDER_SIGMA)
+    assert m.assemble() == 0
+    m.apply_bcs()
+    A_sig = m.block_layout()
+    Fm = m.dptr(L.FEM_F)
+    tsig = {}
+    for kind in ("mixed", "fp64"):
+        u.zero_()
+        flush.fill_(1.0)
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        if kind == "mixed":
+            r = L.MixedResult()
+            rc = lib.nbg_cg_mixed(C.byref(A_sig), Fm, u.data_ptr(), 8 * N, TOL, 0.1,
+                                  L.CG_JACOBI | L.CG_RELATIVE, C.byref(r), ws.data_ptr(),
+                                  ws_bytes, sp)
+        else:
+            r = L.CgResult()
+            rc = lib.nbg_cg_bsr_f64(C.byref(A_sig), Fm, u.data_ptr(), 8 * N, TOL,
+                                    L.CG_JACOBI | L.CG_RELATIVE, C.byref(r), ws.data_ptr(),
+                                    ws_bytes, sp)
+        e1.record(stream)
+        e1.synchronize()
+        assert rc == 0 and r.status == 0
+        t_ = e0.elapsed_time(e1) / 1e3
+        tsig[kind] = {"s_per_solve": t_, "iters": r.niter, "us_per_iter": t_ / r.niter * 1e6}
+    sig_entries = int(A_sig.n_entries)
+    m.close()
     # own rows do not fit in shared memory at this size, so besides the p
     # exchange and 1/Aii (24 B/dof) they move through global memory: per node
     # L1 w out, p in (16 + 16 B), L2 p, w, x, r in (16 + 16 + 16 + 8 B) and
@@ -415,6 +446,10 @@ def run_c3(args):
                         "1e-8 from u=0",
             "nodes": p.n_nodes, "triangles": p.n_elems, "dof": N, "nnz": nnz,
             "block_entries": int(A.n_entries), "blocks": nblk,
+            "block_order": "mesh", "padding": int(A.n_entries) / nblk - 1,
+            "sigma_order": dict(tsig, padding=sig_entries / nblk - 1,
+                                note="SELL-C-sigma node order, sigma 512: fewer stored "
+                                     "entries; not the default (mixed slower)"),
             "setup_s": {"mesh_generation_host": t_gen, "pattern_and_upload": t_create,
                         "assembly_bcs_block_layout": t_asm},
             "mixed": {"s_per_solve": t_mixed, "iters": r_mixed.niter,

@@ -229,7 +229,22 @@ typedef struct {
     const uint16_t *blo;   /* 4 remainder counts per entry */
     const double *dinv64;
     const float *dinv32;
+    /* Optional node order (device, NULL = identity): slice row i holds node
+     * perm[i], iperm[perm[i]] = i, and bcol, dinv and every vector inside the
+     * solvers are in that order.  Sorting the nodes of each window of a few
+     * hundred by row length (SELL-C-sigma) cuts the padding of unstructured
+     * meshes.  The entry points below take and return vectors in the
+     * original node order whatever the order. */
+    const uint32_t *perm;
+    const uint32_t *iperm;
 } nbg_bsr_t;
+
+/* Device: a SELL-C-sigma node order of a node-blocked CSR (row_ptr on the
+ * device): within each window of `sigma` (<= 1024) consecutive nodes, nodes
+ * by descending row length, ties by index; perm / iperm as in nbg_bsr_t and
+ * the slice offsets of that order (n_slices + 1 entries). */
+int nbg_bsr_plan_sigma_dev(uint32_t N_nod, const uint32_t *row_ptr, uint32_t sigma,
+                           uint32_t *perm, uint32_t *iperm, uint32_t *slice_off, void *stream);
 
 /* Host: check the block structure of a CSR and write the slice offsets
  * (n_slices + 1 entries).  NBG_ERR_PATTERN if it is not node-blocked. */
@@ -416,6 +431,17 @@ int nbg_fem_solve(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
                   nbg_cg_result_t *res);
 /* The block layout of K (refilled from the current K values). */
 int nbg_fem_block_layout(nbg_fem_t *f, nbg_bsr_t *out);
+/* Node order of the block layout, fixed at the first nbg_fem_block_layout.
+ * SIGMA sorts each window of `sigma` nodes (0: 512, at most 1024) by row
+ * length.  AUTO is the mesh order: on the 4M-dof T3 L-shape the sigma order
+ * cuts the padding from 44 % to 4 % and the FP64 CG's time per iteration by
+ * 7 %, but the mixed solver's time per iteration rises by 5-8 % (its
+ * gathers lose locality) and its iteration count by 10-15 % (summation
+ * order), so it is taken only on request. */
+#define NBG_ORDER_AUTO 0
+#define NBG_ORDER_MESH 1
+#define NBG_ORDER_SIGMA 2
+int nbg_fem_set_block_order(nbg_fem_t *f, int order, uint32_t sigma);
 /* Fast FP64 CG and mixed-precision CG on the assembled system, x0 = 0. */
 int nbg_fem_solve_fast(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
                        nbg_cg_result_t *res);

@@ -35,7 +35,7 @@ class MixedResult(C.Structure):
 class Bsr(C.Structure):
     _fields_ = [("N", u32), ("Nn", u32), ("n_slices", u32), ("n_entries", u64),
                 ("slice_off", vp), ("bcol", vp), ("b64", vp), ("b32", vp), ("blo", vp), ("dinv64", vp),
-                ("dinv32", vp)]
+                ("dinv32", vp), ("perm", vp), ("iperm", vp)]
 
 
 class SolveInfo(C.Structure):
@@ -81,7 +81,6 @@ SIGS = {
     "nbg_dev_free": ([vp], i32),
     "nbg_h2d": ([vp, vp, sz, vp], i32),
     "nbg_d2h": ([vp, vp, sz, vp], i32),
-    "nbg_d2d": ([vp, vp, sz, vp], i32),
     "nbg_memset": ([vp, i32, sz, vp], i32),
     "nbg_stream_sync": ([vp], i32),
     "nbg_wait_flag": ([vp, i32, u64, vp, vp], i32),
@@ -126,6 +125,9 @@ SIGS = {
     "nbg_cg_mixed": ([C.POINTER(Bsr), vp, vp, u32, f64, f64, C.c_uint,
                       C.POINTER(MixedResult), vp, sz, vp], i32),
     "nbg_fem_block_layout": ([vp, C.POINTER(Bsr)], i32),
+    "nbg_fem_set_block_order": ([vp, i32, u32], i32),
+    "nbg_bsr_plan_sigma_dev": ([u32, vp, u32, vp, vp, vp, vp], i32),
+    "nbg_d2d": ([vp, vp, sz, vp], i32),
     "nbg_fem_solve_fast": ([vp, u32, f64, C.c_uint, C.POINTER(CgResult)], i32),
     "nbg_fem_solve_mixed": ([vp, u32, f64, f64, C.c_uint, C.POINTER(MixedResult)], i32),
     "nbg_solver_create": ([C.POINTER(vp), vp], i32),
@@ -181,6 +183,7 @@ SIGS = {
 (FEM_ROW_PTR, FEM_COL_IDX, FEM_K, FEM_F, FEM_U, FEM_STRAIN, FEM_STRESS, FEM_E, FEM_NOD,
  FEM_CONN, FEM_MAIN_STRESS, FEM_DAMAGE) = range(12)
 CG_JACOBI, CG_RELATIVE = 1, 2
+ORDER_AUTO, ORDER_MESH, ORDER_SIGMA = 0, 1, 2
 METHOD_NBOTS, METHOD_FP64, METHOD_MIXED = 0, 1, 2
 PATTERN_SAME = 1
 

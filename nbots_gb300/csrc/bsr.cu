@@ -11,23 +11,27 @@
 // the 12 B of FP64 CSR.
 #include <cstdint>
 
-#include "common.cuh"
+#include "perm.cuh"
 
 using namespace nbg;
 
 namespace {
 
+// Slice row i holds node v = perm[i] (v = i without an order); columns are
+// stored in the same order (iperm).
 __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
                            const uint32_t* __restrict__ ci, const double* __restrict__ val,
-                           const uint32_t* __restrict__ slice_off, uint32_t* __restrict__ bcol,
-                           double* __restrict__ b64, float* __restrict__ b32,
-                           uint16_t* __restrict__ blo, double* __restrict__ dinv64,
-                           float* __restrict__ dinv32) {
+                           const uint32_t* __restrict__ slice_off,
+                           const uint32_t* __restrict__ perm, const uint32_t* __restrict__ iperm,
+                           uint32_t* __restrict__ bcol, double* __restrict__ b64,
+                           float* __restrict__ b32, uint16_t* __restrict__ blo,
+                           double* __restrict__ dinv64, float* __restrict__ dinv32) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Nn) return;
     const uint32_t s = i >> 5, lane = i & 31;
+    const uint32_t v = perm ? perm[i] : i;
     const uint32_t width = slice_off[s + 1] - slice_off[s];
-    const uint32_t r0 = rp[2 * i], r1 = rp[2 * i + 1];
+    const uint32_t r0 = rp[2 * v], r1 = rp[2 * v + 1];
     const uint32_t nb = (r1 - r0) / 2;
     double d0 = 0.0, d1 = 0.0;
     for (uint32_t k = 0; k < width; k++) {
@@ -35,12 +39,13 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
         double a00 = 0.0, a01 = 0.0, a10 = 0.0, a11 = 0.0;
         uint32_t c = i;
         if (k < nb) {
-            c = ci[r0 + 2 * k] >> 1;
+            const uint32_t w = ci[r0 + 2 * k] >> 1;
+            c = iperm ? iperm[w] : w;
             a00 = val[r0 + 2 * k];
             a01 = val[r0 + 2 * k + 1];
             a10 = val[r1 + 2 * k];
             a11 = val[r1 + 2 * k + 1];
-            if (c == i) {
+            if (w == v) {
                 d0 = a00;
                 d1 = a11;
             }
@@ -152,25 +157,54 @@ extern "C" int nbg_bsr_plan(uint32_t N, const uint32_t* row_ptr, const uint32_t*
 extern "C" int nbg_bsr_fill(const nbg_bsr_t* A, const uint32_t* row_ptr, const uint32_t* col_idx,
                             const double* val, void* stream) {
     if (A->Nn == 0) return NBG_OK;
+    if ((A->perm == nullptr) != (A->iperm == nullptr)) return NBG_ERR_ARG;
     k_bsr_fill<<<(A->Nn + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
-        A->Nn, row_ptr, col_idx, val, A->slice_off, (uint32_t*)A->bcol, (double*)A->b64,
-        (float*)A->b32, (uint16_t*)A->blo, (double*)A->dinv64, (float*)A->dinv32);
+        A->Nn, row_ptr, col_idx, val, A->slice_off, A->perm, A->iperm, (uint32_t*)A->bcol,
+        (double*)A->b64, (float*)A->b32, (uint16_t*)A->blo, (double*)A->dinv64,
+        (float*)A->dinv32);
     NBG_CHECK(cudaGetLastError());
+    return NBG_OK;
+}
+
+// y = A x with x and y in the original node order: with a node order the
+// vectors pass through permuted device copies.
+template <typename T, typename K>
+static int spmv_perm(const nbg_bsr_t* A, const T* x, T* y, cudaStream_t s, K launch) {
+    if (!A->perm) {
+        launch(x, y);
+        NBG_CHECK(cudaGetLastError());
+        return NBG_OK;
+    }
+    T* tmp = nullptr;
+    NBG_CHECK(cudaMalloc(&tmp, 2 * sizeof(T) * (size_t)A->N));
+    cudaError_t e = perm_gather(A->Nn, A->perm, x, tmp, s);
+    if (e == cudaSuccess) {
+        launch(tmp, tmp + A->N);
+        e = cudaGetLastError();
+    }
+    if (e == cudaSuccess) e = perm_scatter(A->Nn, A->perm, tmp + A->N, y, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(tmp);
+    if (e != cudaSuccess) return nbg_cuda_error(e);
     return NBG_OK;
 }
 
 extern "C" int nbg_spmv_bsr_f64(const nbg_bsr_t* A, const double* x, double* y, void* stream) {
     if (A->Nn == 0) return NBG_OK;
-    k_spmv_bsr_f64<<<(A->Nn + 255) / 256, 256, 0, (cudaStream_t)stream>>>(A->Nn, A->slice_off,
-                                                                          A->bcol, A->b64, x, y);
-    NBG_CHECK(cudaGetLastError());
-    return NBG_OK;
+    if (!A->b64) return NBG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    return spmv_perm(A, x, y, s, [&](const double* xx, double* yy) {
+        k_spmv_bsr_f64<<<(A->Nn + 255) / 256, 256, 0, s>>>(A->Nn, A->slice_off, A->bcol, A->b64,
+                                                            xx, yy);
+    });
 }
 
 extern "C" int nbg_spmv_bsr_f32(const nbg_bsr_t* A, const float* x, float* y, void* stream) {
     if (A->Nn == 0) return NBG_OK;
-    k_spmv_bsr_f32<<<(A->Nn + 255) / 256, 256, 0, (cudaStream_t)stream>>>(A->Nn, A->slice_off,
-                                                                          A->bcol, A->b32, x, y);
-    NBG_CHECK(cudaGetLastError());
-    return NBG_OK;
+    if (!A->b32) return NBG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    return spmv_perm(A, x, y, s, [&](const float* xx, float* yy) {
+        k_spmv_bsr_f32<<<(A->Nn + 255) / 256, 256, 0, s>>>(A->Nn, A->slice_off, A->bcol, A->b32,
+                                                            xx, yy);
+    });
 }

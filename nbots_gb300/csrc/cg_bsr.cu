@@ -12,6 +12,7 @@
 // The stop test uses the current gradient norm, not nbots' lagged one.
 #include <cstdint>
 
+#include "perm.cuh"
 #include "persist.cuh"
 
 using namespace nbg;
@@ -178,9 +179,12 @@ done:
     }
 }
 
-size_t cg_bsr_bytes(uint32_t N) {
+size_t cg_bsr_core_bytes(uint32_t N) {
     return 4 * align256((size_t)N * 8) + align256(kMaxBlocks * 3 * 8) * 2 + 3 * 256;
 }
+
+// plus the permuted copies of b and x for a layout with a node order
+size_t cg_bsr_bytes(uint32_t N) { return cg_bsr_core_bytes(N) + perm_tail_bytes(N); }
 
 }  // namespace
 
@@ -224,11 +228,20 @@ extern "C" int nbg_cg_bsr_f64(const nbg_bsr_t* A, const double* b, double* x, ui
     unsigned G = 1;
     double hr[4] = {0, 0, 0, 0};
     cudaError_t e = cudaMemsetAsync(tail, 0, 3 * 256, s);
+    if (A->perm) {  // solve in the layout's node order
+        double* bp = (double*)(base + cg_bsr_core_bytes(A->N));
+        double* xp = bp + align256((size_t)A->N * 8) / 8;
+        if (e == cudaSuccess) e = perm_gather(A->Nn, A->perm, b, bp, s);
+        if (e == cudaSuccess) e = perm_gather(A->Nn, A->perm, (const double*)x, xp, s);
+        a.b = bp;
+        a.x = xp;
+    }
     if (e == cudaSuccess) rc = coop_grid((const void*)k_cg_bsr_f64, A->n_slices, &G);
     if (e == cudaSuccess && rc == NBG_OK) {
         void* args[] = {&a};
         e = cudaLaunchCooperativeKernel((const void*)k_cg_bsr_f64, dim3(G), dim3(kPersistThreads),
                                         args, 0, s);
+        if (e == cudaSuccess && A->perm) e = perm_scatter(A->Nn, A->perm, (const double*)a.x, x, s);
     }
     if (e == cudaSuccess && rc == NBG_OK)
         e = cudaMemcpyAsync(hr, a.res, sizeof(hr), cudaMemcpyDeviceToHost, s);

@@ -32,6 +32,7 @@
 #include <new>
 #include <vector>
 
+#include "perm.cuh"
 #include "persist.cuh"
 
 using namespace nbg;
@@ -552,10 +553,13 @@ uint32_t keep_permille(const nbg_bsr_t& A) {
     return (uint32_t)(1000.0 * budget / stream);
 }
 
-size_t mixed_bytes(uint32_t N) {
+size_t mixed_core_bytes(uint32_t N) {
     const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
     return 5 * f + 2 * h + align256(kMaxBlocks * 6 * 8) + 3 * 256;
 }
+
+// plus the permuted copies of b and x for a layout with a node order
+size_t mixed_bytes(uint32_t N) { return mixed_core_bytes(N) + perm_tail_bytes(N); }
 
 // The mixed solver's SpMV operator as its own launch: w = A p with the split
 // matrix and float-float p, two lanes per node row, the solver's L2 policy
@@ -586,6 +590,7 @@ extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const flo
                                   float* wh, float* wl, void* stream) {
     if (!A || !A->b32 || !A->blo || !ph || !pl || !wh || !wl) return NBG_ERR_ARG;
     if (sizeof(LoP::one) != 4 || sizeof(LoW::one) != 4) return NBG_ERR_ARG;  // FP32 low parts
+    if (A->perm) return NBG_ERR_ARG;  // the operator alone is for layouts in mesh order
     if (A->Nn == 0) return NBG_OK;
     MixArgs a;
     memset(&a, 0, sizeof(a));
@@ -652,6 +657,14 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     size_t dyn = 0;
     double hr[5] = {0, 0, 0, 0, 0};
     cudaError_t e = cudaMemsetAsync(tail, 0, 3 * 256, s);
+    if (A->perm) {  // solve in the layout's node order
+        double* bp = (double*)(base + mixed_core_bytes(A->N));
+        double* xp = bp + align256((size_t)A->N * 8) / 8;
+        if (e == cudaSuccess) e = perm_gather(A->Nn, A->perm, b, bp, s);
+        if (e == cudaSuccess) e = perm_gather(A->Nn, A->perm, (const double*)x, xp, s);
+        a.b = bp;
+        a.u = xp;
+    }
     if (e == cudaSuccess)
         rc = coop_grid_resident((const void*)k_cg_mixed<true>, A->n_slices,
                                 NBG_MIXED_RESIDENT ? kOwnNodeBytes * 32 : 0, &G, &dyn, kMixThreads,
@@ -669,6 +682,7 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
         void* args[] = {&a, &g};
         e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kMixThreads),
                                         args, dyn, s);
+        if (e == cudaSuccess && A->perm) e = perm_scatter(A->Nn, A->perm, (const double*)a.u, x, s);
     }
     if (e == cudaSuccess && rc == NBG_OK)
         e = cudaMemcpyAsync(hr, g.res, sizeof(hr), cudaMemcpyDeviceToHost, s);
@@ -944,7 +958,7 @@ extern "C" int nbg_mixed_batch_create(nbg_mixed_batch_t** out, const nbg_bsr_t* 
                                       const double* b, double* x, uint32_t n_sys,
                                       const uint32_t* slice_ptr, uint32_t max_iter, double tol,
                                       double delta, unsigned flags, void* stream) {
-    if (!out) return NBG_ERR_ARG;
+    if (!out || !A || A->perm) return NBG_ERR_ARG;  // instances own contiguous slices
     *out = nullptr;
     if (!A || !b || !x || !slice_ptr || n_sys == 0 || n_sys > kMaxBlocks || !A->b64 ||
         !A->b32 || !A->blo || !A->dinv32 || !(delta > 0.0 && delta < 1.0))

@@ -201,6 +201,38 @@ __global__ void k_slice_width(uint32_t N_nod, uint32_t S, const uint32_t* __rest
     w[s] = m;
 }
 
+// SELL-C-sigma order: one block per window of sigma nodes; each node's place
+// is the number of nodes of its window with a longer row, or as long a row
+// and a smaller index.
+__global__ void __launch_bounds__(1024)
+    k_sigma_perm(uint32_t N_nod, uint32_t sigma, const uint32_t* __restrict__ rp,
+                 uint32_t* __restrict__ perm, uint32_t* __restrict__ iperm) {
+    __shared__ uint32_t w[1024];
+    const uint32_t s0 = blockIdx.x * sigma, t = threadIdx.x;
+    const uint32_t n = min(sigma, N_nod - s0);
+    const uint32_t v = s0 + t;
+    const uint32_t wv = t < n ? rp[2 * (size_t)v + 1] - rp[2 * (size_t)v] : 0u;
+    w[t] = wv;
+    __syncthreads();
+    if (t >= n) return;
+    uint32_t rank = 0;
+    for (uint32_t u = 0; u < n; u++) rank += (w[u] > wv) || (w[u] == wv && u < t);
+    perm[s0 + rank] = v;
+    iperm[v] = s0 + rank;
+}
+
+__global__ void k_slice_width_perm(uint32_t N_nod, uint32_t S, const uint32_t* __restrict__ perm,
+                                   const uint32_t* __restrict__ rp, uint32_t* __restrict__ w) {
+    const uint32_t s = blockIdx.x * blockDim.x + threadIdx.x;
+    if (s >= S) return;
+    uint32_t m = 0;
+    for (uint32_t i = 32 * s; i < N_nod && i < 32 * s + 32; i++) {
+        const uint32_t v = perm[i];
+        m = max(m, (rp[2 * (size_t)v + 1] - rp[2 * (size_t)v]) / 2);
+    }
+    w[s] = m;
+}
+
 // Exclusive scan of n values into out[0..n], out[n] the total; tmp needs
 // scan_tmp_words(n) words.
 size_t scan_tmp_words(uint32_t n) {
@@ -329,6 +361,27 @@ extern "C" int nbg_pattern_dev(uint32_t nen, uint32_t N_nod, uint32_t N_elem, ui
 done:
     if (ci) cudaFree(ci);
     if (nbr) cudaFree(nbr);
+    cudaFree(ws);
+    return rc;
+}
+
+extern "C" int nbg_bsr_plan_sigma_dev(uint32_t N_nod, const uint32_t* row_ptr, uint32_t sigma,
+                                      uint32_t* perm, uint32_t* iperm, uint32_t* slice_off,
+                                      void* stream) {
+    if (N_nod == 0 || sigma == 0 || sigma > 1024 || !perm || !iperm || !slice_off)
+        return NBG_ERR_ARG;
+    cudaStream_t s = (cudaStream_t)stream;
+    const uint32_t S = (N_nod + 31) / 32;
+    const size_t tmp_words = scan_tmp_words(S);
+    uint32_t* ws = nullptr;
+    NBG_CHECK(cudaMalloc(&ws, 4 * ((size_t)S + tmp_words)));
+    int rc = NBG_OK;
+    k_sigma_perm<<<nblk(N_nod, sigma), sigma, 0, s>>>(N_nod, sigma, row_ptr, perm, iperm);
+    k_slice_width_perm<<<nblk(S, 256), 256, 0, s>>>(N_nod, S, perm, row_ptr, ws);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess) rc = scan_exclusive(ws, slice_off, S, ws + S, s);
+    if (e == cudaSuccess && rc == NBG_OK) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) rc = nbg_cuda_error(e);
     cudaFree(ws);
     return rc;
 }

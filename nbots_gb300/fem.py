@@ -111,6 +111,9 @@ class FemSystem:
             L.check(rc, "fem_solve_mixed")
         return r
 
+    def set_block_order(self, order, sigma=0):
+        L.check(self.lib.nbg_fem_set_block_order(self.handle, order, sigma), "set_block_order")
+
     def block_layout(self):
         b = L.Bsr()
         L.check(self.lib.nbg_fem_block_layout(self.handle, C.byref(b)), "block_layout")

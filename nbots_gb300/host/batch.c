@@ -207,6 +207,8 @@ int nbg_batch_create(nbg_batch_t **out, uint32_t n, const nbg_mesh_t *meshes,
 	b->bcs.N_bc = (uint32_t)ib;
 	b->bcs.bc = b->bc;
 	TRY(nbg_fem_create(&b->f, &b->m, stream));
+	/* each instance owns a contiguous range of slices: mesh order */
+	TRY(nbg_fem_set_block_order(b->f, NBG_ORDER_MESH, 0));
 	TRY(nbg_dev_alloc((void **)&b->d_rho, 8 * (Ne ? Ne : 1)));
 	TRY(nbg_dev_alloc((void **)&b->d_dJ, 8 * (Ne ? Ne : 1)));
 	*out = b;

@@ -252,7 +252,8 @@ void nbg_fem_destroy(nbg_fem_t *f)
 		     f->damage,
 		     f->conn, f->row_ptr, f->col_idx, f->inc_ptr, f->inc_elem, f->distorted,
 		     f->inc_local, f->enabled, f->matched, f->status, f->cg_ws,
-		     f->slice_off, f->bcol, f->b64, f->dinv64, f->b32, f->dinv32, f->blo};
+		     f->slice_off, f->bcol, f->b64, f->dinv64, f->b32, f->dinv32, f->blo,
+		     f->perm, f->iperm};
 	for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++)
 		nbg_dev_free(p[i]);
 	free(f);
@@ -521,11 +522,47 @@ int nbg_fem_solve(nbg_fem_t *f, uint32_t max_iter, double tol, unsigned flags,
 			  res, f->cg_ws, f->cg_ws_bytes, f->stream);
 }
 
+int nbg_fem_set_block_order(nbg_fem_t *f, int order, uint32_t sigma)
+{
+	if (!f || order < NBG_ORDER_AUTO || order > NBG_ORDER_SIGMA || sigma > 1024)
+		return NBG_ERR_ARG;
+	if (f->b64)  /* fixed by the first layout */
+		return order == f->block_order ? NBG_OK : NBG_ERR_ARG;
+	f->block_order = order;
+	f->block_sigma = sigma;
+	return NBG_OK;
+}
+
+/* The SELL-C-sigma order (pattern.cu). */
+static int choose_order(nbg_fem_t *f)
+{
+	int rc = NBG_OK;
+	const uint32_t Nn = f->m.N_nod, S = f->bsr.n_slices;
+	uint32_t *so = NULL;
+	TRY(nbg_dev_alloc((void **)&f->perm, 4 * (size_t)Nn));
+	TRY(nbg_dev_alloc((void **)&f->iperm, 4 * (size_t)Nn));
+	TRY(nbg_dev_alloc((void **)&so, 4 * ((size_t)S + 1)));
+	TRY(nbg_bsr_plan_sigma_dev(Nn, f->row_ptr, f->block_sigma ? f->block_sigma : 512, f->perm,
+				   f->iperm, so, f->stream));
+	uint32_t w_sigma = 0;
+	TRY(nbg_d2h(&w_sigma, so + S, 4, f->stream));
+	TRY(nbg_d2d(f->slice_off, so, 4 * ((size_t)S + 1), f->stream));
+	TRY(nbg_stream_sync(f->stream));
+	f->bsr.n_entries = 32ull * w_sigma;  /* bcol keeps its larger allocation */
+	f->bsr.perm = f->perm;
+	f->bsr.iperm = f->iperm;
+fail:
+	nbg_dev_free(so);
+	return rc;
+}
+
 int nbg_fem_block_layout(nbg_fem_t *f, nbg_bsr_t *out)
 {
 	int rc = NBG_OK;
 	if (!f->bsr_ok)
 		return NBG_ERR_PATTERN;
+	if (!f->b64 && f->block_order == NBG_ORDER_SIGMA)
+		TRY(choose_order(f));
 	const uint64_t ent = f->bsr.n_entries;
 	if (!f->b64) {
 		TRY(nbg_dev_alloc((void **)&f->b64, 32 * ent));

@@ -46,6 +46,7 @@ def test_lshape_assembly_and_solvers_on_gpu():
     O.set_bconditions(fl, rp, ci, K_ref, F_ref)
     r["K_bc"], r["F_bc"] = K_ref, F_ref
     s = FemSystem(p)
+    s.set_block_order(L.ORDER_SIGMA)
     assert s.assemble() == 0
     K_asm, F_asm = s.get(L.FEM_K), s.get(L.FEM_F)
     assert np.array_equal(s.get(L.FEM_ROW_PTR), r["row_ptr"])
@@ -61,12 +62,22 @@ def test_lshape_assembly_and_solvers_on_gpu():
     # nbots does; on this mesh (re-entrant corner) the true residual of FP64
     # CG levels off near 1e-10, so it is checked at 1e-10 with a factor 2 for
     # that gap.  The mixed solver judges the recomputed FP64 residual itself.
-    for solve, tol, slack, uerr in ((s.solve_fast, 1e-10, 2.0, 1e-7),
-                                    (s.solve_mixed, 1e-11, 1.05, 1e-8)):
-        res = solve(tol=tol)
-        assert res.status == 0
-        u = s.get(L.FEM_U)
-        rr = np.linalg.norm(F - O.spmv(rp, ci, K, u)) / np.linalg.norm(F)
-        assert rr <= slack * tol, (solve.__name__, rr)
-        assert np.linalg.norm(u - tight) / np.linalg.norm(tight) < uerr
+    # the solvers on a layout in SELL-C-sigma node order and in mesh order
+    # (the default); the mesh order stores about 40 % more entries here
+    m = FemSystem(p)
+    assert m.assemble() == 0
+    m.apply_bcs()
+    A_sigma, A_mesh = s.block_layout(), m.block_layout()
+    assert A_sigma.perm and not A_mesh.perm
+    assert A_sigma.n_entries < 0.8 * A_mesh.n_entries
+    for sys_ in (s, m):
+        for solve, tol, slack, uerr in ((sys_.solve_fast, 1e-10, 2.0, 1e-7),
+                                        (sys_.solve_mixed, 1e-11, 1.05, 1e-8)):
+            res = solve(tol=tol)
+            assert res.status == 0
+            u = sys_.get(L.FEM_U)
+            rr = np.linalg.norm(F - O.spmv(rp, ci, K, u)) / np.linalg.norm(F)
+            assert rr <= slack * tol, (solve.__name__, rr)
+            assert np.linalg.norm(u - tight) / np.linalg.norm(tight) < uerr
+    m.close()
     s.close()
