@@ -155,6 +155,14 @@ void nb_fem_compute_2D_Non_Linear_Solid_Mechanics(const nb_mesh2D_t *part,
 						  nb_analysis2D_params *params2D,
 						  nb_fem_implicit_t *params, const char *logfile);
 
+/* A/B switch: with NBG_DROPIN_CPU=1 in the environment every replaced
+ * compute entry (SpMV, the two CGs, the FEM entries, stress, principal
+ * stresses, the damage solve) calls the next definition of its symbol in
+ * link order -- nbots' own CPU code when libnbots.so follows this library --
+ * on the same objects.  Unset (the default) the GPU path runs.  Set, with no
+ * next definition loaded, the call fails with NBG_ERR_ARG. */
+int nbg_dropin_cpu(void);
+
 /* Last error of a drop-in call that nbots would have ended with exit(1)
  * (0 if none); cleared by reading. */
 int nbg_dropin_error(void);

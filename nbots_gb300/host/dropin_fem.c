@@ -9,13 +9,15 @@
  * evaluates them (set_bconditions.c:63-260): segment nodes, vertex nodes for
  * Dirichlet, and (0,0) for Neumann vertex loads.
  */
-#define _GNU_SOURCE
-#include <dlfcn.h>
 #include <stdlib.h>
 #include <string.h>
 
 #include "nbots_dropin.h"
 #include "nbots_gb300.h"
+
+void nbg_dropin_record_error(int e);
+int nbg_dropin_cpu(void);
+void *nbg_dropin_next(const char *name);
 
 typedef struct {
 	nbg_mesh_t m;
@@ -168,6 +170,16 @@ int nb_fem_compute_2D_Solid_Mechanics(const nb_mesh2D_t *part, const nb_fem_elem
 				      const bool *elements_enabled, double *displacement,
 				      double *strain)
 {
+	if (nbg_dropin_cpu()) {
+		typedef int (*fn_t)(const nb_mesh2D_t *, const nb_fem_elem_t *,
+				    const nb_material_t *, const nb_bcond_t *, bool, double[2],
+				    nb_analysis2D_t, nb_analysis2D_params *, const bool *, double *,
+				    double *);
+		fn_t next = (fn_t)nbg_dropin_next("nb_fem_compute_2D_Solid_Mechanics");
+		return next ? next(part, elemtype, material, bcond, enable_self_weight, gravity,
+				   analysis2D, params2D, elements_enabled, displacement, strain)
+			    : NBG_ERR_ARG;
+	}
 	(void)analysis2D;
 	const uint32_t nen = nb_fem_elem_get_N_nodes(elemtype);
 	if (nen != 3 && nen != 4)
@@ -232,6 +244,17 @@ void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t 
 				       double *strain, const bool *elements_enabled,
 				       double *stress)
 {
+	if (nbg_dropin_cpu()) {
+		typedef void (*fn_t)(uint32_t, const nb_fem_elem_t *, const nb_material_t *,
+				     nb_analysis2D_t, double *, const bool *, double *);
+		fn_t next = (fn_t)nbg_dropin_next("nb_fem_compute_stress_from_strain");
+		if (next)
+			next(N_elements, elemtype, material, analysis2D, strain, elements_enabled,
+			     stress);
+		else
+			nbg_dropin_record_error(NBG_ERR_ARG);
+		return;
+	}
 	(void)analysis2D;
 	const uint32_t nen = nb_fem_elem_get_N_nodes(elemtype);
 	const size_t ng = nen == 4 ? 4 : 1;
@@ -268,6 +291,15 @@ void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t 
 void pipeline_compute_main_stress(double *stress, double *main_stress, uint32_t N_elements,
 				  const nb_fem_elem_t *const elem)
 {
+	if (nbg_dropin_cpu()) {
+		typedef void (*fn_t)(double *, double *, uint32_t, const nb_fem_elem_t *const);
+		fn_t next = (fn_t)nbg_dropin_next("pipeline_compute_main_stress");
+		if (next)
+			next(stress, main_stress, N_elements, elem);
+		else
+			nbg_dropin_record_error(NBG_ERR_ARG);
+		return;
+	}
 	const uint32_t nen = nb_fem_elem_get_N_nodes(elem);
 	const size_t n = (size_t)nb_fem_elem_get_N_gpoints(elem) * N_elements;
 	void *ds = NULL, *dm = NULL;
@@ -281,7 +313,6 @@ void pipeline_compute_main_stress(double *stress, double *main_stress, uint32_t 
 	nbg_dev_free(dm);
 }
 
-void nbg_dropin_record_error(int e);
 
 typedef void (*nonlinear_fn)(const nb_mesh2D_t *, const nb_fem_elem_t *, const nb_material_t *,
 			     const nb_bcond_t *, bool, double[2], bool, nb_analysis2D_t,
@@ -296,13 +327,18 @@ void nb_fem_compute_2D_Non_Linear_Solid_Mechanics(const nb_mesh2D_t *part,
 						  nb_analysis2D_params *params2D,
 						  nb_fem_implicit_t *params, const char *logfile)
 {
-	if (enable_Cholesky_solver) {
-		/* the direct-solver branch is nbots' own */
-		nonlinear_fn next = (nonlinear_fn)dlsym(
-			RTLD_NEXT, "nb_fem_compute_2D_Non_Linear_Solid_Mechanics");
+	if (enable_Cholesky_solver || nbg_dropin_cpu()) {
+		/* the direct-solver branch is nbots' own; so is everything under the
+		 * A/B switch */
+		nonlinear_fn next = (nonlinear_fn)nbg_dropin_next(
+			"nb_fem_compute_2D_Non_Linear_Solid_Mechanics");
 		if (next) {
-			next(part, elem, material, bcond, enable_self_weight, gravity, true,
-			     analysis2D, params2D, params, logfile);
+			next(part, elem, material, bcond, enable_self_weight, gravity,
+			     enable_Cholesky_solver, analysis2D, params2D, params, logfile);
+			return;
+		}
+		if (nbg_dropin_cpu()) {
+			nbg_dropin_record_error(NBG_ERR_ARG);
 			return;
 		}
 	}

@@ -10,6 +10,8 @@
  * entirely that way (nb_free_mem is free(), memory_bot/allocate_mem.c).
  */
 #define _POSIX_C_SOURCE 200809L
+#define _GNU_SOURCE
+#include <dlfcn.h>
 #include <pthread.h>
 #include <stdio.h>
 #include <stdlib.h>
@@ -44,6 +46,27 @@ void nbg_dropin_record_error(int e)
 	if (e)
 		g_err = e;
 }
+
+/* A/B switch: with NBG_DROPIN_CPU=1 in the environment, the replaced
+ * compute entry points call the next definition of the same symbol in link
+ * order -- nbots' own CPU code when libnbots.so follows this library -- so
+ * both paths run on the same objects.  Off unless set; with it set and no
+ * such definition loaded, the call fails with NBG_ERR_ARG instead of running
+ * anything. */
+int nbg_dropin_cpu(void)
+{
+	const char *v = getenv("NBG_DROPIN_CPU");
+	return v && v[0] == '1' && v[1] == 0;
+}
+
+void *nbg_dropin_next(const char *name)
+{
+	return dlsym(RTLD_NEXT, name);
+}
+
+typedef int (*cg_fn)(const nb_sparse_t *, const double *, double *, uint32_t, double,
+		     uint32_t *, double *, uint32_t);
+typedef void (*spmv_fn)(const nb_sparse_t *, const double *, double *, uint32_t);
 
 static void reg_add(const nb_sparse_t *A, double *v, uint32_t *ix, uint64_t nnz)
 {
@@ -378,6 +401,11 @@ int nb_sparse_solve_CG_precond_Jacobi(const nb_sparse_t *A, const double *b, dou
 				      uint32_t *niter_performed, double *tolerance_reached,
 				      uint32_t omp_parallel_threads)
 {
+	if (nbg_dropin_cpu()) {
+		cg_fn next = (cg_fn)nbg_dropin_next("nb_sparse_solve_CG_precond_Jacobi");
+		return next ? next(A, b, x, max_iter, tolerance, niter_performed,
+				   tolerance_reached, omp_parallel_threads) : NBG_ERR_ARG;
+	}
 	(void)omp_parallel_threads;
 	return solve(A, b, x, max_iter, tolerance, niter_performed, tolerance_reached,
 		     NBG_CG_JACOBI);
@@ -388,6 +416,11 @@ int nb_sparse_solve_conjugate_gradient(const nb_sparse_t *A, const double *b, do
 				       uint32_t *niter_performed, double *tolerance_reached,
 				       uint32_t omp_parallel_threads)
 {
+	if (nbg_dropin_cpu()) {
+		cg_fn next = (cg_fn)nbg_dropin_next("nb_sparse_solve_conjugate_gradient");
+		return next ? next(A, b, x, max_iter, tolerance, niter_performed,
+				   tolerance_reached, omp_parallel_threads) : NBG_ERR_ARG;
+	}
 	(void)omp_parallel_threads;
 	return solve(A, b, x, max_iter, tolerance, niter_performed, tolerance_reached, 0);
 }
@@ -395,6 +428,14 @@ int nb_sparse_solve_conjugate_gradient(const nb_sparse_t *A, const double *b, do
 void nb_sparse_multiply_vector(const nb_sparse_t *A, const double *in, double *out,
 			       uint32_t omp_parallel_threads)
 {
+	if (nbg_dropin_cpu()) {
+		spmv_fn next = (spmv_fn)nbg_dropin_next("nb_sparse_multiply_vector");
+		if (next)
+			next(A, in, out, omp_parallel_threads);
+		else
+			g_err = NBG_ERR_ARG;
+		return;
+	}
 	(void)omp_parallel_threads;
 	flat_t f;
 	if (flatten(A, &f) != NBG_OK) {
