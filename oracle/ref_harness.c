@@ -437,6 +437,28 @@ static int run_problem(const char *in, const char *out, uint32_t threads)
 	dump_f64("cg7_tol_reached", t7);
 	dump_i32("cg7_status", cg7);
 
+	/* nb_sparse_solve_Gauss_Seidel (gauss_seidel.c:14-58): 40 sweeps from the
+	 * SpMV input (tolerance 0 is never met), and up to 2000 sweeps from 0 to
+	 * the absolute tolerance 1e-6 */
+	{
+		double *xg = xalloc(8 * (size_t)N);
+		memcpy(xg, xs, 8 * (size_t)N);
+		uint32_t gi = 0;
+		double ge = 0;
+		int gst = nb_sparse_solve_Gauss_Seidel(K, F, xg, 40, 0.0, &gi, &ge, 1);
+		dump("gs40_x", DT_F64, xg, N);
+		dump_u32("gs40_niter", gi);
+		dump_f64("gs40_error", ge);
+		dump_i32("gs40_status", gst);
+		memset(xg, 0, 8 * (size_t)N);
+		gst = nb_sparse_solve_Gauss_Seidel(K, F, xg, 2000, 1e-6, &gi, &ge, 1);
+		dump("gs_x", DT_F64, xg, N);
+		dump_u32("gs_niter", gi);
+		dump_f64("gs_error", ge);
+		dump_i32("gs_status", gst);
+		free(xg);
+	}
+
 	/* pipeline.c:266-278 */
 	uint32_t ngp = nb_fem_elem_get_N_gpoints(elem);
 	double *strain = xalloc(8 * 3 * (size_t)ngp * p.N_elem);

@@ -65,6 +65,21 @@ def test_oracle_log_equals_reference(name):
         assert n_gs == 0 and recs[-1][1][2]
 
 
+def test_oracle_gauss_seidel_equals_reference(golden):
+    """The oracle's Gauss-Seidel equals nbots' own run bit for bit: 40 sweeps
+    from the SpMV input, and 2000 sweeps from 0 at tolerance 1e-6 (iterate,
+    sweep count, error, status)."""
+    name, p, d = golden
+    if "gs40_x" not in d:
+        return
+    rp, ci, K, F = d["row_ptr"], d["col_idx"], d["K_bc"], d["F_bc"]
+    for x0, mi, tol, key in ((d["spmv_x"], 40, 0.0, "gs40"), (None, 2000, 1e-6, "gs")):
+        x, it, err, st = O.gauss_seidel(rp, ci, K, F, x0=x0, max_iter=mi, tol=tol)
+        assert np.array_equal(x.view(np.uint64), d[key + "_x"].view(np.uint64)), (name, key)
+        assert (it, st) == (int(d[key + "_niter"][0]), int(d[key + "_status"][0]))
+        assert err == float(d[key + "_error"][0])
+
+
 def test_oracle_gauss_seidel_stops_on_tolerance():
     """A diagonally dominant system converges; the returned error is below
     tol and another sweep from the result does not start."""
@@ -123,6 +138,20 @@ def gs_gpu(rp, ci, K, b, x0, max_iter, tol):
                                   C.byref(res), ws.ptr, None)
     assert rc == 0
     return arrs[4].numpy(), res
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", ["q4_allbc_16x8", "t3_beam_cantilever", "c1_q4_64x32"])
+def test_gpu_gauss_seidel_equals_reference(name):
+    """Device Gauss-Seidel against nbots' own runs: iterates bit for bit."""
+    _, d = load_golden(name)
+    rp, ci, K, F = d["row_ptr"], d["col_idx"], d["K_bc"], d["F_bc"]
+    for x0, mi, tol, key in ((d["spmv_x"], 40, 0.0, "gs40"),
+                             (np.zeros(F.shape[0]), 2000, 1e-6, "gs")):
+        x, r = gs_gpu(rp, ci, K, F, x0, mi, tol)
+        assert np.array_equal(x.view(np.uint64), d[key + "_x"].view(np.uint64)), key
+        assert (r.niter, r.status) == (int(d[key + "_niter"][0]), int(d[key + "_status"][0]))
+        assert abs(r.error - float(d[key + "_error"][0])) <= 1e-12 * float(d[key + "_error"][0])
 
 
 @pytest.mark.gpu
