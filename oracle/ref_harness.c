@@ -427,6 +427,19 @@ static int run_problem(const char *in, const char *out, uint32_t threads)
 	dump_f64("cg_tol_reached", tol_reached);
 	dump_i32("cg_status", cg);
 
+	/* unpreconditioned CG (conjugate_gradient.c:13-77), same settings */
+	{
+		double *up = xalloc(8 * (size_t)N);
+		uint32_t np_ = 0;
+		double tp = 0;
+		int cgp = nb_sparse_solve_conjugate_gradient(K, F, up, N, 1e-8, &np_, &tp, 1);
+		dump("u_plain", DT_F64, up, N);
+		dump_u32("cgp_niter", np_);
+		dump_f64("cgp_tol_reached", tp);
+		dump_i32("cgp_status", cgp);
+		free(up);
+	}
+
 	/* a short run (max_iter = 7) pins the not-converged return path */
 	double *u7 = xalloc(8 * (size_t)N);
 	uint32_t n7 = 0;

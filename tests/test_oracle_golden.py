@@ -41,6 +41,10 @@ def test_oracle_stages_bit_exact(golden):
     assert it == int(d["cg_niter"][0]) and cst == int(d["cg_status"][0])
     assert same(np.array([tr]), d["cg_tol_reached"])
     assert same(u, d["u"]), name
+    # unpreconditioned CG (conjugate_gradient.c:13-77)
+    up, itp, trp, stp = O.cg_jacobi(rp, ci, K, F, plain=True)
+    assert (itp, stp) == (int(d["cgp_niter"][0]), int(d["cgp_status"][0]))
+    assert same(up, d["u_plain"]) and same(np.array([trp]), d["cgp_tol_reached"])
     u7, it7, tr7, st7 = O.cg_jacobi(rp, ci, K, F, max_iter=7)
     assert (it7, st7) == (int(d["cg7_niter"][0]), int(d["cg7_status"][0])) == (7, 1)
     assert same(u7, d["u_it7"]) and same(np.array([tr7]), d["cg7_tol_reached"])
