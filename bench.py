@@ -820,6 +820,13 @@ def run_profile(args):
     s = FemSystem(p)
     assert s.assemble() == 0
     s.apply_bcs()
+    if args.profile == "nbots":
+        # the drop-in's solver (nbots' iteration, FP64, CSR), `iters` iterations
+        for _ in range(2):
+            r = s.solve(max_iter=args.iters)
+        print(json.dumps({"profile": "nbots", "iters": r.niter, "dof": s.N}))
+        s.close()
+        return 0
     A = s.block_layout()
     N = s.N
     F = s.dptr(L.FEM_F)
@@ -875,7 +882,7 @@ def main():
     ap.add_argument("--c3", action="store_true",
                     help="run the 4M-dof unstructured T3 L-shape instead (mesh generation "
                          "takes about a minute on the host)")
-    ap.add_argument("--profile", choices=["mixed", "fp64", "spmv", "damage", "pattern"],
+    ap.add_argument("--profile", choices=["mixed", "fp64", "spmv", "damage", "pattern", "nbots"],
                     help="one bounded kernel launch for ncu instead of the benchmark")
     ap.add_argument("--iters", type=int, default=100)
     args = ap.parse_args()
