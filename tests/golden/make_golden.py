@@ -64,6 +64,9 @@ def small_cases():
     ]
     cases[p.name] = p
 
+    # the smallest cantilever: two elements, six nodes
+    cases["q4_tiny_1x2"] = W.cantilever_q4(1, 2, name="q4_tiny_1x2")
+
     # a distorted element (detJ < 0): assembly must fail with status 1
     p = W.cantilever_q4(8, 4, name="q4_distorted_8x4")
     nid = 2 * 9 + 3

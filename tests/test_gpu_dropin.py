@@ -55,7 +55,8 @@ def test_cg_precond_jacobi(G, name):
     x7 = np.zeros(p.n_dof)
     st7 = G.nb_sparse_solve_CG_precond_Jacobi(A, b.ctypes.data, x7.ctypes.data, 7, 1e-8,
                                                C.byref(it), C.byref(tr), 1)
-    assert (st7, it.value) == (1, 7) and rel(x7, d["u_it7"]) < 1e-12
+    assert (st7, it.value) == (int(d["cg7_status"][0]), int(d["cg7_niter"][0]))
+    assert rel(x7, d["u_it7"]) < (1e-12 if st7 else 1e-10)
     G.nb_sparse_destroy(A)
 
 

@@ -46,7 +46,9 @@ def test_oracle_stages_bit_exact(golden):
     assert (itp, stp) == (int(d["cgp_niter"][0]), int(d["cgp_status"][0]))
     assert same(up, d["u_plain"]) and same(np.array([trp]), d["cgp_tol_reached"])
     u7, it7, tr7, st7 = O.cg_jacobi(rp, ci, K, F, max_iter=7)
-    assert (it7, st7) == (int(d["cg7_niter"][0]), int(d["cg7_status"][0])) == (7, 1)
+    assert (it7, st7) == (int(d["cg7_niter"][0]), int(d["cg7_status"][0]))
+    if int(d["cg_niter"][0]) > 7:  # the not-converged return path
+        assert (it7, st7) == (7, 1)
     assert same(u7, d["u_it7"]) and same(np.array([tr7]), d["cg7_tol_reached"])
     assert same(O.strain(fl, u), d["strain"])
     if "fem_u" in d:
