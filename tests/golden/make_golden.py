@@ -83,6 +83,11 @@ DAMAGE_CASES = {
     # every conjugate-gradient solve fails and falls back to Gauss-Seidel,
     # which fails too (the absolute tolerance 1e-8 is out of reach)
     "dmg_t3_beam150": ("beam150", 1e4, 10.0, 2, 30, 5, 1e-6),
+    # edge settings: no iteration allowed, a cap of three iterations with a
+    # break at the first residual that is not a new best, and no load step
+    "dmg_q4_16x8_noiter": ("q4", 6.0, 10.0, 2, 0, 6, 1e-7),
+    "dmg_q4_16x8_cap": ("q4", 6.0, 10.0, 3, 3, 1, 1e-7),
+    "dmg_q4_16x8_nosteps": ("q4", 6.0, 10.0, 0, 5, 5, 1e-7),
 }
 
 

@@ -22,7 +22,9 @@ import pytest
 from conftest import load_golden
 from oracle import oracle as O
 
-CASES = ["dmg_q4_16x8", "dmg_t3_beam150"]
+CASES = ["dmg_q4_16x8", "dmg_t3_beam150", "dmg_q4_16x8_noiter", "dmg_q4_16x8_cap",
+         "dmg_q4_16x8_nosteps"]
+EDGE = ["dmg_q4_16x8_noiter", "dmg_q4_16x8_cap", "dmg_q4_16x8_nosteps"]
 
 
 def params(d):
@@ -61,6 +63,8 @@ def test_oracle_log_equals_reference(name):
     recs = parse(ref)
     if name == "dmg_t3_beam150":
         assert n_gs > 0 and any(k == "fail" for k, _ in recs)
+    elif name == "dmg_q4_16x8_nosteps":
+        assert recs == [("head", ())]
     else:
         assert n_gs == 0 and recs[-1][1][2]
 
@@ -216,6 +220,26 @@ def test_gpu_damage_q4(tmp_path):
     check_q4_run(log, s.get(L.FEM_U), s.get(L.FEM_DAMAGE), p, d)
     assert info.gs_fallbacks == 0 and info.cg_solves > 0
     assert info.iterations == sum(step_iterations(parse(log)))
+    s.close()
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("name", EDGE)
+def test_gpu_damage_edge_settings(tmp_path, name):
+    """No iteration, an iteration cap with a break on the first residual that
+    is not a new best, no load step: the same records as nbots."""
+    from nbots_gb300.fem import FemSystem
+    p, d = load_golden(name)
+    s = FemSystem(p)
+    logf = tmp_path / "edge.log"
+    s.damage(*params(d), logfile=logf)
+    got = parse(logf.read_text())
+    ref = parse(bytes(d["damage_log"]).decode())
+    assert [k for k, _ in got] == [k for k, _ in ref]
+    for (k, a), (_, b) in zip(got, ref):
+        if k == "res":
+            assert a[0] == b[0] and a[2] == b[2]
+            assert abs(a[1] - b[1]) <= 1e-6 * abs(b[1]) + 1e-8, (a, b)
     s.close()
 
 
