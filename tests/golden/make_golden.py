@@ -88,10 +88,17 @@ DAMAGE_CASES = {
     "dmg_q4_16x8_noiter": ("q4", 6.0, 10.0, 2, 0, 6, 1e-7),
     "dmg_q4_16x8_cap": ("q4", 6.0, 10.0, 3, 3, 1, 1e-7),
     "dmg_q4_16x8_nosteps": ("q4", 6.0, 10.0, 0, 5, 5, 1e-7),
+    # self weight, function-valued loads, a prescribed displacement (the
+    # q4_allbc_16x8 problem), below the damage threshold
+    "dmg_q4_allbc": ("allbc", 100.0, 50.0, 3, 30, 5, 1e-7),
 }
 
 
 def damage_problem(src, tmp, a):
+    if src == "allbc":
+        path = os.path.join(tmp, "dmg_allbc.bin")
+        P.write_problem(small_cases()["q4_allbc_16x8"], path)
+        return path
     if src == "q4":
         p = W.cantilever_q4(16, 8, point_load=-0.5, name="dmg_q4_16x8")
         path = os.path.join(tmp, "dmg_q4.bin")

@@ -23,8 +23,8 @@ from conftest import load_golden
 from oracle import oracle as O
 
 CASES = ["dmg_q4_16x8", "dmg_t3_beam150", "dmg_q4_16x8_noiter", "dmg_q4_16x8_cap",
-         "dmg_q4_16x8_nosteps"]
-EDGE = ["dmg_q4_16x8_noiter", "dmg_q4_16x8_cap", "dmg_q4_16x8_nosteps"]
+         "dmg_q4_16x8_nosteps", "dmg_q4_allbc"]
+EDGE = ["dmg_q4_16x8_noiter", "dmg_q4_16x8_cap", "dmg_q4_16x8_nosteps", "dmg_q4_allbc"]
 
 
 def params(d):
@@ -227,7 +227,8 @@ def test_gpu_damage_q4(tmp_path):
 @pytest.mark.parametrize("name", EDGE)
 def test_gpu_damage_edge_settings(tmp_path, name):
     """No iteration, an iteration cap with a break on the first residual that
-    is not a new best, no load step: the same records as nbots."""
+    is not a new best, no load step, and self weight with every boundary
+    condition form: the same records as nbots."""
     from nbots_gb300.fem import FemSystem
     p, d = load_golden(name)
     s = FemSystem(p)
