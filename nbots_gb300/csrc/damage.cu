@@ -278,7 +278,7 @@ __global__ void __launch_bounds__(kGsThreads) k_gauss_seidel(GsArgs a) {
         block_sum_f64<1>(v, buf, t);
         if (threadIdx.x == 0) {
             s_err = t[0];
-            s_stop = !(t[0] > tol2);
+            s_stop = t[0] <= tol2;  // as nbots: a NaN error keeps sweeping
             if (!s_stop && a.time_limit_ns && gtimer() - t0 > a.time_limit_ns) s_stop = 2;
         }
         __syncthreads();
