@@ -201,26 +201,36 @@ def bench_damage(L, W, with_cpu):
     1e-7, ft = 6, Gf = 10, E = 1.  Wall time of nbg_fem_damage (device
     assembly with damage, boundary conditions, residual, nbots-order Jacobi
     PCG, strain and damage, host log) against the oracle's one-thread
-    restatement of nbots' loop on the same problem."""
+    restatement of nbots' loop on the same problem; and the same device loop
+    with the fast FP64 block CG as its inner solver."""
     import tempfile
     from nbots_gb300.fem import FemSystem
     out = {}
     args_ = (6.0, 10.0, 4, 40, 6, 1e-7)
+    for method in (L.METHOD_NBOTS, L.METHOD_FP64):  # warm: modules, first launches
+        s = FemSystem(W.cantilever_q4(16, 8, point_load=0.0, top_traction=0.35))
+        s.damage(*args_, method=method)
+        s.close()
     for nx, ny, cpu in ((128, 64, with_cpu), (512, 256, False)):
         p = W.cantilever_q4(nx, ny, point_load=0.0, top_traction=0.35)
-        s = FemSystem(p)
-        with tempfile.TemporaryDirectory() as td:
-            logf = os.path.join(td, "dmg.log")
-            s.damage(*args_, logfile=None)  # warm (module load, workspaces)
-            t0 = time.perf_counter()
-            info = s.damage(*args_, logfile=logf)
-            t_gpu = time.perf_counter() - t0
-            log = open(logf).read()
-        s.close()
-        row = {"workload": f"Q4 cantilever {nx}x{ny}, {p.n_dof} dof, top traction 0.35",
-               "gpu_s": t_gpu, "iterations": info.iterations, "cg_solves": info.cg_solves,
-               "cg_iterations": info.cg_iterations, "gs_fallbacks": info.gs_fallbacks,
-               "step_iterations": _damage_step_iters(log)}
+        row = {"workload": f"Q4 cantilever {nx}x{ny}, {p.n_dof} dof, top traction 0.35"}
+        for method, key in ((L.METHOD_NBOTS, "nbots_cg"), (L.METHOD_FP64, "fast_fp64_cg")):
+            s = FemSystem(p)
+            with tempfile.TemporaryDirectory() as td:
+                logf = os.path.join(td, "dmg.log")
+                t0 = time.perf_counter()
+                info = s.damage(*args_, logfile=logf, method=method)
+                t_gpu = time.perf_counter() - t0
+                log = open(logf).read()
+            s.close()
+            res = {"gpu_s": t_gpu, "iterations": info.iterations,
+                   "cg_solves": info.cg_solves, "cg_iterations": info.cg_iterations,
+                   "gs_fallbacks": info.gs_fallbacks,
+                   "step_iterations": _damage_step_iters(log)}
+            if method == L.METHOD_NBOTS:
+                row.update(res)  # the drop-in's inner solver: the row's headline
+            else:
+                row[key] = res
         if cpu:
             from oracle import oracle as O
             t0 = time.perf_counter()
@@ -228,7 +238,7 @@ def bench_damage(L, W, with_cpu):
             t_cpu = time.perf_counter() - t0
             row.update(cpu_oracle_s=t_cpu, cpu_cores=1,
                        cpu_step_iterations=_damage_step_iters(olog),
-                       speedup=t_cpu / t_gpu)
+                       speedup=t_cpu / row["gpu_s"])
         out[f"{nx}x{ny}"] = row
     return out
 

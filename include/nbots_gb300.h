@@ -473,11 +473,15 @@ typedef struct {
  * iterations without a new best residual.  Appends nbots' log lines to
  * `logfile` (NULL: no log).  Displacements end in NBG_FEM_U, damage in
  * NBG_FEM_DAMAGE, strain in NBG_FEM_STRAIN.  Returns 0, NBG_DISTORTED, or an
- * error; Gauss-Seidel stops with NBG_ERR_TIMEOUT after 600 s. */
+ * error; Gauss-Seidel stops with NBG_ERR_TIMEOUT after 600 s.  method: the
+ * inner solver, NBG_METHOD_NBOTS (nbots' iteration on the CSR, the drop-in's
+ * choice) or NBG_METHOD_FP64 (the fast FP64 CG on the block layout, refilled
+ * after every assembly; it stops on the current residual norm instead of
+ * nbots' lagged one). */
 int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, double thickness,
                    double density, int self_weight, const double gravity[2], double ft,
                    double gf, uint32_t n_steps, uint32_t max_iter, uint32_t max_iter_noenh,
-                   double rtol, const char *logfile, nbg_damage_info_t *info);
+                   double rtol, int method, const char *logfile, nbg_damage_info_t *info);
 
 /* ------------------------------------------------------------------ SIMP */
 /* SIMP element sensitivities (no counterpart in nbots): with

@@ -98,7 +98,7 @@ SIGS = {
     "nbg_gauss_seidel_f64": ([u32, vp, vp, vp, vp, vp, vp, vp, u32, u32, f64, f64,
                               C.POINTER(GsResult), vp, vp], i32),
     "nbg_fem_damage": ([vp, vp, f64, f64, f64, f64, i32, vp, f64, f64, u32, u32, u32, f64,
-                        C.c_char_p, C.POINTER(DamageInfo)], i32),
+                        i32, C.c_char_p, C.POINTER(DamageInfo)], i32),
     "nbg_gather_assemble_f64": ([u32, u32, u32, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp, vp],
                                 i32),
     "nbg_apply_increments_f64": ([u32, vp, vp, vp, vp, vp], i32),

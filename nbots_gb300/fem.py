@@ -131,16 +131,17 @@ class FemSystem:
         L.check(self.lib.nbg_fem_main_stress(self.handle), "main_stress")
         return self.get(L.FEM_MAIN_STRESS)
 
-    def damage(self, ft, gf, n_steps, max_iter, max_iter_noenh, rtol, logfile=None):
+    def damage(self, ft, gf, n_steps, max_iter, max_iter_noenh, rtol, logfile=None,
+               method=L.METHOD_NBOTS):
         """nbots' quasi-static damage solve (static_damage2D.c:239-470) with
         material E = p.E[0]; returns the run's counters.  The log goes to
-        `logfile` (appended) when given."""
+        `logfile` (appended) when given; `method` picks the inner solver."""
         p = self.p
         info = L.DamageInfo()
         rc = self.lib.nbg_fem_damage(self.handle, C.byref(self.h.bcs), float(p.E[0]), p.nu,
                                      p.thickness, p.density, int(p.self_weight),
                                      _p(self.h.grav), ft, gf, n_steps, max_iter,
-                                     max_iter_noenh, rtol,
+                                     max_iter_noenh, rtol, method,
                                      None if logfile is None else str(logfile).encode(),
                                      C.byref(info))
         L.check(rc, "fem_damage")

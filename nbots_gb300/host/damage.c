@@ -69,14 +69,15 @@ static void logf_append(FILE *lf, const char *fmt, ...)
 }
 
 typedef struct {
-	double *du, *res, *r, *r_prev, *norm2, *rws, *gws;
+	double *du, *res, *r, *r_prev, *norm2, *rws, *gws, *bws;
 	uint32_t *lev_ptr, *lev_rows, n_levels;
 	int have_levels;
 } dmg_ws_t;
 
 static void free_ws(dmg_ws_t *w)
 {
-	void *p[] = {w->du, w->res, w->r, w->r_prev, w->rws, w->gws, w->lev_ptr, w->lev_rows};
+	void *p[] = {w->du, w->res, w->r, w->r_prev, w->rws, w->gws, w->bws, w->lev_ptr,
+		     w->lev_rows};
 	for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++)
 		nbg_dev_free(p[i]);
 }
@@ -112,10 +113,10 @@ fail:
 int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, double thickness,
 		   double density, int self_weight, const double gravity[2], double ft,
 		   double gf, uint32_t n_steps, uint32_t max_iter, uint32_t max_iter_noenh,
-		   double rtol, const char *logfile, nbg_damage_info_t *info)
+		   double rtol, int method, const char *logfile, nbg_damage_info_t *info)
 {
 	int rc = NBG_OK;
-	if (!f || !bcs)
+	if (!f || !bcs || (method != NBG_METHOD_NBOTS && method != NBG_METHOD_FP64))
 		return NBG_ERR_ARG;
 	nbg_damage_info_t inf;
 	memset(&inf, 0, sizeof(inf));
@@ -140,6 +141,9 @@ int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, doub
 	TRY(nbg_dev_alloc((void **)&w.rws, nbg_residual_workspace_bytes(N) + 8));
 	w.norm2 = w.rws + nbg_residual_workspace_bytes(N) / 8;
 	TRY(nbg_fem_cg_workspace(f));
+	const size_t bws_bytes = nbg_cg_bsr_workspace_bytes(N);
+	if (method == NBG_METHOD_FP64)
+		TRY(nbg_dev_alloc((void **)&w.bws, bws_bytes));
 	Eh = malloc(8 * (size_t)(ne ? ne : 1));
 	rh = malloc(8 * (npt ? npt : 1));
 	if (!Eh || !rh)
@@ -189,9 +193,15 @@ int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, doub
 			}
 			/* returns 1 (and cg.status 1) when the tolerance is not reached */
 			nbg_cg_result_t cg;
-			const int st = nbg_cg_f64(N, f->row_ptr, f->col_idx, f->K, w.res, w.du, N,
-						  1e-8, NBG_CG_JACOBI, &cg, f->cg_ws,
-						  f->cg_ws_bytes, f->stream);
+			int st;
+			if (method == NBG_METHOD_FP64) {
+				TRY(nbg_fem_block_layout(f, NULL));  /* from this K */
+				st = nbg_cg_bsr_f64(&f->bsr, w.res, w.du, N, 1e-8, NBG_CG_JACOBI, &cg,
+						    w.bws, bws_bytes, f->stream);
+			} else {
+				st = nbg_cg_f64(N, f->row_ptr, f->col_idx, f->K, w.res, w.du, N, 1e-8,
+						NBG_CG_JACOBI, &cg, f->cg_ws, f->cg_ws_bytes, f->stream);
+			}
 			if (st < 0)
 				TRY(st);
 			if (cg.status < 0)

@@ -367,7 +367,8 @@ void nb_fem_compute_2D_Non_Linear_Solid_Mechanics(const nb_mesh2D_t *part,
 				    nb_fem_implicit_get_N_steps(params),
 				    nb_fem_implicit_get_N_max_iter(params),
 				    nb_fem_implicit_get_N_max_iter_without_enhance(params),
-				    nb_fem_implicit_get_residual_tolerance(params), logfile, &info);
+				    nb_fem_implicit_get_residual_tolerance(params), NBG_METHOD_NBOTS,
+				    logfile, &info);
 	}
 	nbg_dropin_record_error(rc);
 	nbg_fem_destroy(f);

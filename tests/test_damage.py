@@ -209,13 +209,14 @@ def check_q4_run(log, u, dmg, p, d):
 
 
 @pytest.mark.gpu
-def test_gpu_damage_q4(tmp_path):
+@pytest.mark.parametrize("method", [0, 1])  # nbots' CG on the CSR, fast FP64 CG
+def test_gpu_damage_q4(tmp_path, method):
     from nbots_gb300 import _lib as L
     from nbots_gb300.fem import FemSystem
     p, d = load_golden("dmg_q4_16x8")
     s = FemSystem(p)
     logf = tmp_path / "dmg.log"
-    info = s.damage(*params(d), logfile=logf)
+    info = s.damage(*params(d), logfile=logf, method=method)
     log = logf.read_text()
     check_q4_run(log, s.get(L.FEM_U), s.get(L.FEM_DAMAGE), p, d)
     assert info.gs_fallbacks == 0 and info.cg_solves > 0
