@@ -147,9 +147,23 @@ __global__ void __launch_bounds__(kThreads) k_cg_f64(CgArgs a) {
                 }
             } else {
                 for (uint32_t r = r0 + threadIdx.x; r < r1; r += kThreads) {
+                    // four columns, values and gathers in flight, then the
+                    // four ordered adds
+                    const uint32_t ke = rp[r + 1];
+                    uint32_t kk = rp[r];
                     double s = 0.0;
-                    for (uint32_t kk = rp[r]; kk < rp[r + 1]; kk++)
-                        s = add(s, mul(val[kk], p[ci[kk]]));
+                    for (; kk + 4 <= ke; kk += 4) {
+                        const uint32_t c0 = ci[kk], c1 = ci[kk + 1], c2 = ci[kk + 2],
+                                       c3 = ci[kk + 3];
+                        const double v0 = val[kk], v1 = val[kk + 1], v2 = val[kk + 2],
+                                     v3 = val[kk + 3];
+                        const double x0 = p[c0], x1 = p[c1], x2 = p[c2], x3 = p[c3];
+                        s = add(s, mul(v0, x0));
+                        s = add(s, mul(v1, x1));
+                        s = add(s, mul(v2, x2));
+                        s = add(s, mul(v3, x3));
+                    }
+                    for (; kk < ke; kk++) s = add(s, mul(val[kk], p[ci[kk]]));
                     a.w[r] = s;
                     const double gi = a.g[r], qi = a.q[r];
                     v3[0] = add(v3[0], mul(p[r], s));
