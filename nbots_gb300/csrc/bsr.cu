@@ -8,7 +8,9 @@
 // 32 consecutive blocks per step (coalesced), one node row per lane; padding
 // entries point at the row's own node with zero values.  One uint32 column
 // serves four values, so FP32 values + index cost 5 B per nonzero instead of
-// the 12 B of FP64 CSR.
+// the 12 B of FP64 CSR.  The standalone SpMVs unroll the slice walk by four
+// and load the matrix with an L2 evict_first policy: at 1M dof (L2 flushed)
+// the FP32 one took 25.2 us against 31.4 us for the plain loop.
 #include <cstdint>
 
 #include "perm.cuh"
@@ -92,11 +94,13 @@ __global__ void __launch_bounds__(256) k_spmv_bsr_f64(uint32_t Nn, const uint32_
     const uint32_t k0 = so[s], k1 = so[s + 1];
     const double2* __restrict__ xv = reinterpret_cast<const double2*>(x);
     const double2* __restrict__ bv = reinterpret_cast<const double2*>(b64);
+    const uint64_t pol = l2_policy(false);  // the matrix streams through L2 once
     double y0 = 0.0, y1 = 0.0;
+#pragma unroll 4
     for (uint32_t k = k0; k < k1; k++) {
         const size_t e = (size_t)k * 32 + lane;
-        const double2 xc = xv[bcol[e]];
-        const double2 top = bv[2 * e], bot = bv[2 * e + 1];
+        const double2 xc = xv[ld_hint(bcol + e, pol)];
+        const double2 top = ld_hint(bv + 2 * e, pol), bot = ld_hint(bv + 2 * e + 1, pol);
         y0 = fma(top.x, xc.x, y0);
         y0 = fma(top.y, xc.y, y0);
         y1 = fma(bot.x, xc.x, y1);
@@ -116,11 +120,13 @@ __global__ void __launch_bounds__(256) k_spmv_bsr_f32(uint32_t Nn, const uint32_
     const uint32_t k0 = so[s], k1 = so[s + 1];
     const float2* __restrict__ xv = reinterpret_cast<const float2*>(x);
     const float4* __restrict__ bv = reinterpret_cast<const float4*>(b32);
+    const uint64_t pol = l2_policy(false);  // the matrix streams through L2 once
     float y0 = 0.f, y1 = 0.f;
+#pragma unroll 4
     for (uint32_t k = k0; k < k1; k++) {
         const size_t e = (size_t)k * 32 + lane;
-        const float2 xc = xv[bcol[e]];
-        const float4 a = bv[e];
+        const float4 a = ld_hint(bv + e, pol);
+        const float2 xc = xv[ld_hint(bcol + e, pol)];
         y0 = fmaf(a.x, xc.x, y0);
         y0 = fmaf(a.y, xc.y, y0);
         y1 = fmaf(a.z, xc.x, y1);
