@@ -244,13 +244,16 @@ __device__ __forceinline__ void group_reduce0(const double* part, uint32_t G, do
 __device__ __forceinline__ double2 spmv_row_f64(const nbg_bsr_t& A, uint32_t s, uint32_t lane,
                                                 const double2* __restrict__ xv) {
     const double2* __restrict__ bv = reinterpret_cast<const double2*>(A.b64);
+    // the 36 B/block matrix stream passes through L2 once per iteration;
+    // evict_first keeps the vectors there (1M dof: 64.3 -> 62.8 us/iteration)
+    const uint64_t pol = l2_policy(false);
     double y0 = 0.0, y1 = 0.0;
     const uint32_t k0 = A.slice_off[s], k1 = A.slice_off[s + 1];
 #pragma unroll 3
     for (uint32_t k = k0; k < k1; k++) {
         const size_t e = (size_t)k * 32 + lane;
-        const double2 xc = xv[A.bcol[e]];
-        const double2 top = bv[2 * e], bot = bv[2 * e + 1];
+        const double2 xc = xv[ld_hint(A.bcol + e, pol)];
+        const double2 top = ld_hint(bv + 2 * e, pol), bot = ld_hint(bv + 2 * e + 1, pol);
         y0 = fma(top.x, xc.x, y0);
         y0 = fma(top.y, xc.y, y0);
         y1 = fma(bot.x, xc.x, y1);
