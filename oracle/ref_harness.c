@@ -427,6 +427,21 @@ static int run_problem(const char *in, const char *out, uint32_t threads)
 	dump_f64("cg_tol_reached", tol_reached);
 	dump_i32("cg_status", cg);
 
+	/* the same Jacobi-PCG from a non-zero initial guess (the damage loop
+	 * passes the previous increment, static_damage2D.c:410) */
+	{
+		double *ux = xalloc(8 * (size_t)N);
+		memcpy(ux, xs, 8 * (size_t)N);
+		uint32_t nx = 0;
+		double tx = 0;
+		int cgx = nb_sparse_solve_CG_precond_Jacobi(K, F, ux, N, 1e-8, &nx, &tx, 1);
+		dump("u_x0", DT_F64, ux, N);
+		dump_u32("cgx0_niter", nx);
+		dump_f64("cgx0_tol_reached", tx);
+		dump_i32("cgx0_status", cgx);
+		free(ux);
+	}
+
 	/* unpreconditioned CG (conjugate_gradient.c:13-77), same settings */
 	{
 		double *up = xalloc(8 * (size_t)N);

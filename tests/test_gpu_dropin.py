@@ -51,6 +51,13 @@ def test_cg_precond_jacobi(G, name):
     assert st == int(d["cg_status"][0])
     assert cg_iters_close(it.value, int(d["cg_niter"][0]), np.linalg.norm(b))
     assert rel(x, d["u"]) < 1e-10
+    # from a non-zero initial guess (the damage loop passes the last increment)
+    xg = np.ascontiguousarray(d["spmv_x"]).copy()
+    stx = G.nb_sparse_solve_CG_precond_Jacobi(A, b.ctypes.data, xg.ctypes.data, p.n_dof, 1e-8,
+                                               C.byref(it), C.byref(tr), 1)
+    assert stx == int(d["cgx0_status"][0])
+    assert cg_iters_close(it.value, int(d["cgx0_niter"][0]), np.linalg.norm(b))
+    assert rel(xg, d["u_x0"]) < 1e-10
     # the not-converged return path (max_iter = 7)
     x7 = np.zeros(p.n_dof)
     st7 = G.nb_sparse_solve_CG_precond_Jacobi(A, b.ctypes.data, x7.ctypes.data, 7, 1e-8,

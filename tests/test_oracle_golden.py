@@ -41,6 +41,10 @@ def test_oracle_stages_bit_exact(golden):
     assert it == int(d["cg_niter"][0]) and cst == int(d["cg_status"][0])
     assert same(np.array([tr]), d["cg_tol_reached"])
     assert same(u, d["u"]), name
+    # from a non-zero initial guess (the damage loop's case)
+    ux, itx, trx, stx = O.cg_jacobi(rp, ci, K, F, x0=d["spmv_x"])
+    assert (itx, stx) == (int(d["cgx0_niter"][0]), int(d["cgx0_status"][0]))
+    assert same(ux, d["u_x0"]) and same(np.array([trx]), d["cgx0_tol_reached"])
     # unpreconditioned CG (conjugate_gradient.c:13-77)
     up, itp, trp, stp = O.cg_jacobi(rp, ci, K, F, plain=True)
     assert (itp, stp) == (int(d["cgp_niter"][0]), int(d["cgp_status"][0]))
