@@ -275,7 +275,6 @@ int nbg_fem_create(nbg_fem_t **out, const nbg_mesh_t *m, void *stream)
 	f->stream = stream;
 	f->N = 2 * m->N_nod;
 	const size_t ne = m->N_elem, nen = m->nen, Nn = m->N_nod;
-	const size_t nd = 2 * nen;
 	const uint32_t S = (m->N_nod + 31) / 32;
 	void *edg_d = NULL;
 	TRY(nbg_dev_alloc((void **)&f->nod, 16 * Nn));
@@ -322,7 +321,6 @@ int nbg_fem_create(nbg_fem_t **out, const nbg_mesh_t *m, void *stream)
 		f->bsr_ok = 1;
 	}
 	TRY(nbg_stream_sync(stream));
-	(void)nd;
 	*out = f;
 	return NBG_OK;
 fail:
