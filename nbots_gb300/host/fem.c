@@ -383,6 +383,7 @@ int nbg_fem_apply_bcs(nbg_fem_t *f, const nbg_bcs_t *b, double factor)
 {
 	int rc = NBG_OK;
 	plan_t p;
+	memset(&p, 0, sizeof(p));  /* the fail path frees its arrays */
 	uint32_t *gidx = NULL, *gptr = NULL, *order = NULL, *cnt = NULL;
 	uint32_t *ev_ptr = NULL, *ev_of = NULL;
 	double *ginc = NULL;
