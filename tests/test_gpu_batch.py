@@ -130,3 +130,36 @@ def test_not_converged_is_reported(L, batch):
     res, _ = b.results()
     assert all(r.status == 1 and r.niter == 3 for r in res)
     b.setup(max_iter=20000, tol=1e-10)
+
+
+def test_t3_batch(L):
+    """Unstructured T3 instances (L-shapes of three sizes, uneven row
+    lengths, padded slices): merged assembly bit for bit with each single
+    system, and the batched solve within 1e-8 of FP64 solves."""
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.batch import Batch
+    probs = [W.t3_lshape(n, seed=30 + n) for n in (1500, 2500, 4000)]
+    rng = np.random.default_rng(8)
+    rho = [rng.uniform(0.3, 0.9, p.n_elems) for p in probs]
+    b = Batch(probs)
+    b.assemble_simp(rho, nu=probs[0].nu, thickness=probs[0].thickness)
+    b.setup(max_iter=40000, tol=1e-10)
+    rp, ci, K = (b.merged(w) for w in (L.FEM_ROW_PTR, L.FEM_COL_IDX, L.FEM_K))
+    E = b.merged(L.FEM_E)
+    b.launch()
+    res, J = b.results()
+    us = b.displacements()
+    for k, p in enumerate(probs):
+        no = 2 * int(b.node_off[k])
+        e0, e1 = int(b.elem_off[k]), int(b.elem_off[k + 1])
+        s = single(L, p, E[e0:e1].copy())
+        r0, r1 = no, no + p.n_dof
+        seg = slice(int(rp[r0]), int(rp[r1]))
+        assert np.array_equal(ci[seg] - no, s.get(L.FEM_COL_IDX))
+        assert np.array_equal(K[seg].view(np.uint64), s.get(L.FEM_K).view(np.uint64))
+        assert res[k].status == 0 and res[k].relres <= 1e-10, k
+        assert s.solve_fast(tol=1e-13).status == 0
+        u64 = s.get(L.FEM_U)
+        assert np.linalg.norm(us[k] - u64) / np.linalg.norm(u64) < 1e-8, k
+        s.close()
+    b.close()
