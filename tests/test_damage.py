@@ -10,8 +10,9 @@ sweep's per-row arithmetic is nbots'; only the error sum is ordered
 differently); the device damage loop, through the C ABI and through the
 drop-in symbol, takes the same iterations per load step as nbots and its
 residuals agree with nbots' to 1e-6 relative plus the inner solves'
-absolute tolerance 1e-8, displacements and damage with the oracle's to 1e-6.  The conjugate-gradient solves inside are the device CG, whose
-sums run in another order than nbots', so the run is not bit-exact.
+absolute tolerance 1e-8, displacements and damage with the oracle's to
+1e-6.  The conjugate-gradient solves inside are the device CG, whose sums
+run in another order than nbots', so the run is not bit-exact.
 """
 import ctypes as C
 import re
