@@ -491,6 +491,9 @@ int nbg_simp_sensitivity_f64(uint32_t nen, uint32_t N_elem, const double *nod,
                              const uint32_t *conn, double nu, double thickness,
                              const double *rho, double penal, double E0, double Emin,
                              const double *a, const double *b, double *out, void *stream);
+/* The SIMP moduli E[e] = Emin + rho[e]^p (E0 - Emin) (device arrays). */
+int nbg_simp_modulus_f64(uint32_t N_elem, const double *rho, double penal, double E0,
+                         double Emin, double *E, void *stream);
 
 #define NBG_SIMP_COMPLIANCE 0   /* J = F^T u (self-adjoint) */
 #define NBG_SIMP_DOF 1          /* J = u[dof], one adjoint solve K lambda = e_dof */

@@ -136,6 +136,7 @@ SIGS = {
     "nbg_solver_solve": ([vp, vp, vp, u32, f64, C.c_uint, i32, C.POINTER(SolveInfo)], i32),
     "nbg_host_alloc": ([C.POINTER(vp), sz], i32),
     "nbg_host_free": ([vp], i32),
+    "nbg_simp_modulus_f64": ([u32, vp, f64, f64, f64, vp, vp], i32),
     "nbg_simp_sensitivity_f64": ([u32, u32, vp, vp, f64, f64, vp, f64, f64, f64, vp, vp, vp,
                                   vp], i32),
     "nbg_fem_simp": ([vp, vp, vp, f64, f64, f64, f64, f64, i32, u32, f64, i32, vp,

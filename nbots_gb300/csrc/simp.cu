@@ -93,7 +93,23 @@ __global__ void __launch_bounds__(128) k_simp_sens(uint32_t N_elem, const double
     out[e] = -dE * s;
 }
 
+// E_e = Emin + rho_e^p (E0 - Emin), rounded step by step (no contraction).
+__global__ void k_simp_modulus(uint32_t n, const double* __restrict__ rho, double penal,
+                               double E0, double Emin, double* __restrict__ E) {
+    const uint32_t e = blockIdx.x * blockDim.x + threadIdx.x;
+    if (e < n) E[e] = nbg::add(Emin, nbg::mul(pow(rho[e], penal), nbg::sub(E0, Emin)));
+}
+
 }  // namespace
+
+extern "C" int nbg_simp_modulus_f64(uint32_t N_elem, const double* rho, double penal, double E0,
+                                    double Emin, double* E, void* stream) {
+    if (N_elem == 0) return NBG_OK;
+    k_simp_modulus<<<(N_elem + 255) / 256, 256, 0, (cudaStream_t)stream>>>(N_elem, rho, penal,
+                                                                          E0, Emin, E);
+    NBG_CHECK(cudaGetLastError());
+    return NBG_OK;
+}
 
 extern "C" int nbg_simp_sensitivity_f64(uint32_t nen, uint32_t N_elem, const double* nod,
                                         const uint32_t* conn, double nu, double thickness,

@@ -253,7 +253,7 @@ void nbg_fem_destroy(nbg_fem_t *f)
 		     f->conn, f->row_ptr, f->col_idx, f->inc_ptr, f->inc_elem, f->distorted,
 		     f->inc_local, f->enabled, f->matched, f->status, f->cg_ws,
 		     f->slice_off, f->bcol, f->b64, f->dinv64, f->b32, f->dinv32, f->blo,
-		     f->perm, f->iperm};
+		     f->perm, f->iperm, f->simp_rho, f->simp_out, f->simp_e, f->simp_lam};
 	for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++)
 		nbg_dev_free(p[i]);
 	free(f);
@@ -333,6 +333,8 @@ int nbg_fem_assemble(nbg_fem_t *f, const double *E, double nu, double thickness,
 		     double density, int self_weight, const double gravity[2],
 		     const uint8_t *enabled)
 {
+	if (!E)
+		return NBG_ERR_ARG;
 	return nbg_fem_assemble_dev_damage(f, E, nu, thickness, density, self_weight, gravity,
 					   enabled, NULL);
 }
@@ -349,7 +351,8 @@ int nbg_fem_assemble_dev_damage(nbg_fem_t *f, const double *E, double nu, double
 	}
 	f->nu = nu;
 	f->has_enabled = enabled != NULL;
-	TRY(nbg_h2d(f->E, E, 8 * ne, f->stream));
+	if (E)  /* else the moduli are already in f->E */
+		TRY(nbg_h2d(f->E, E, 8 * ne, f->stream));
 	if (enabled)
 		TRY(nbg_h2d(f->enabled, enabled, ne, f->stream));
 	uint32_t init = 0xffffffffu;
@@ -744,27 +747,28 @@ int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double n
 {
 	int rc = NBG_OK;
 	const uint32_t Ne = f->m.N_elem, N = f->N;
-	double *E = malloc(8 * (size_t)(Ne ? Ne : 1));
 	double *hu = malloc(8 * (size_t)N), *hF = malloc(8 * (size_t)N);
-	void *d_rho = NULL, *d_lam = NULL, *d_e = NULL, *d_out = NULL;
 	memset(info, 0, sizeof(*info));
-	if (!E || !hu || !hF)
+	if (!hu || !hF)
 		TRY(NBG_ERR_NOMEM);
 	if (objective == NBG_SIMP_DOF && dof >= N)
 		TRY(NBG_ERR_ARG);
-	for (uint32_t e = 0; e < Ne; e++)
-		E[e] = Emin + pow(rho[e], penal) * (E0 - Emin);
+	/* device buffers kept across calls: an optimisation loop calls this
+	 * once per design update */
+	if (!f->simp_rho) {
+		TRY(nbg_dev_alloc((void **)&f->simp_rho, 8 * (size_t)(Ne ? Ne : 1)));
+		TRY(nbg_dev_alloc((void **)&f->simp_out, 8 * (size_t)(Ne ? Ne : 1)));
+	}
+	TRY(nbg_h2d(f->simp_rho, rho, 8 * (size_t)Ne, f->stream));
+	TRY(nbg_simp_modulus_f64(Ne, f->simp_rho, penal, E0, Emin, f->E, f->stream));
 	double g0[2] = {0.0, 0.0};
-	TRY(nbg_fem_assemble(f, E, nu, thickness, 0.0, 0, g0, NULL));
+	TRY(nbg_fem_assemble_dev_damage(f, NULL, nu, thickness, 0.0, 0, g0, NULL, NULL));
 	TRY(nbg_fem_apply_bcs(f, bcs, 1.0));
 	TRY(zero_u(f));
 	TRY(solve_rhs(f, f->F, f->u, tol, method, &info->fwd_iters));
 	TRY(nbg_d2h(hu, f->u, 8 * (size_t)N, f->stream));
 	TRY(nbg_d2h(hF, f->F, 8 * (size_t)N, f->stream));
 	TRY(nbg_stream_sync(f->stream));
-	TRY(nbg_dev_alloc(&d_rho, 8 * (size_t)(Ne ? Ne : 1)));
-	TRY(nbg_dev_alloc(&d_out, 8 * (size_t)(Ne ? Ne : 1)));
-	TRY(nbg_h2d(d_rho, rho, 8 * (size_t)Ne, f->stream));
 	const double *adj = f->u;
 	if (objective == NBG_SIMP_COMPLIANCE) {
 		double J = 0.0;
@@ -777,25 +781,22 @@ int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double n
 		memset(hF, 0, 8 * (size_t)N);
 		hF[dof] = 1.0;
 		memset(hu, 0, 8 * (size_t)N);
-		TRY(nbg_dev_alloc(&d_e, 8 * (size_t)N));
-		TRY(nbg_dev_alloc(&d_lam, 8 * (size_t)N));
-		TRY(nbg_h2d(d_e, hF, 8 * (size_t)N, f->stream));
-		TRY(nbg_h2d(d_lam, hu, 8 * (size_t)N, f->stream));
-		TRY(solve_rhs(f, d_e, d_lam, tol, method, &info->adj_iters));
-		adj = d_lam;
+		if (!f->simp_e) {
+			TRY(nbg_dev_alloc((void **)&f->simp_e, 8 * (size_t)N));
+			TRY(nbg_dev_alloc((void **)&f->simp_lam, 8 * (size_t)N));
+		}
+		TRY(nbg_h2d(f->simp_e, hF, 8 * (size_t)N, f->stream));
+		TRY(nbg_h2d(f->simp_lam, hu, 8 * (size_t)N, f->stream));
+		TRY(solve_rhs(f, f->simp_e, f->simp_lam, tol, method, &info->adj_iters));
+		adj = f->simp_lam;
 	}
-	TRY(nbg_simp_sensitivity_f64(f->m.nen, Ne, f->nod, f->conn, nu, thickness, d_rho, penal,
-				     E0, Emin, adj, f->u, d_out, f->stream));
-	TRY(nbg_d2h(dJ, d_out, 8 * (size_t)Ne, f->stream));
+	TRY(nbg_simp_sensitivity_f64(f->m.nen, Ne, f->nod, f->conn, nu, thickness, f->simp_rho,
+				     penal, E0, Emin, adj, f->u, f->simp_out, f->stream));
+	TRY(nbg_d2h(dJ, f->simp_out, 8 * (size_t)Ne, f->stream));
 	TRY(nbg_stream_sync(f->stream));
 fail:
 	info->status = rc;
-	free(E);
 	free(hu);
 	free(hF);
-	nbg_dev_free(d_rho);
-	nbg_dev_free(d_lam);
-	nbg_dev_free(d_e);
-	nbg_dev_free(d_out);
 	return rc;
 }

@@ -33,9 +33,11 @@ struct nbg_fem {
 	int block_order;           /* NBG_ORDER_* */
 	uint32_t block_sigma;      /* SELL-C-sigma window, 0: default */
 	uint32_t *perm, *iperm;    /* the block layout's node order, or NULL */
+	double *simp_rho, *simp_out, *simp_e, *simp_lam;  /* nbg_fem_simp buffers */
 };
 
-/* Assembly with an optional device array of damage per Gauss point. */
+/* Assembly with an optional device array of damage per Gauss point; E NULL
+ * means the moduli are already in f->E. */
 int nbg_fem_assemble_dev_damage(nbg_fem_t *f, const double *E, double nu, double thickness,
 				double density, int self_weight, const double gravity[2],
 				const uint8_t *enabled, const double *damage);
