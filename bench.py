@@ -243,6 +243,27 @@ def bench_damage(L, W, with_cpu):
     return out
 
 
+def bench_fem_entry(W):
+    """nbots' FEM entry through the drop-in symbol (nb_fem_compute_2D_Solid_
+    Mechanics with nbots' objects built by the host library): the 1024x512
+    cantilever with one material (E = 1, the entry takes one), host arrays in
+    and out, pattern, assembly, boundary conditions, nbots-order Jacobi-PCG
+    (x0 = 0, max_iter = N, absolute 1e-8) and strain, wall time."""
+    from nbots_gb300.dropin import NbotsObjects
+    warm = NbotsObjects(W.cantilever_q4(16, 8))
+    warm.fem()
+    warm.close()
+    p = W.config_c2()
+    p.E = np.ones(p.n_elems)
+    ob = NbotsObjects(p)
+    t0 = time.perf_counter()
+    st, u, strain = ob.fem()
+    t = time.perf_counter() - t0
+    ob.close()
+    return {"workload": "C2 mesh and loads, one material E = 1", "status": int(st),
+            "s_per_call": t, "max_abs_u": float(np.max(np.abs(u)))}
+
+
 def bench_c5(args, lib, L, W, sp, dev, stream, flush):
     """96 batched SIMP cantilevers: one graph launch = zero u, batched mixed
     CG to relres 1e-8 per instance, compliance sensitivities.  Per-instance
@@ -736,6 +757,7 @@ def run_gpu(args):
     # ---- max over ranks
     t_all, e2e_all = R.max_over_ranks([t_med, e2e_v], device=dev)
 
+    fem_entry = None if args.no_c4 else bench_fem_entry(W)
     c4 = None if args.no_c4 else bench_c4(lib, L, W)
     c5 = None if args.no_c5 else bench_c5(args, lib, L, W, sp, dev, stream, flush)
     dmg = None if args.no_damage else bench_damage(L, W, rank == 0 and not args.no_cpu_baseline)
@@ -785,6 +807,7 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(8 * N),
                     "path": "nbg_solver_set_matrix (values, pattern kept) + nbg_solver_solve "
                             "(mixed) from pinned host buffers"},
+            "fem_entry_dropin": fem_entry,
             "c4_simp": c4,
             "c5_batch": c5,
             "damage": dmg,
