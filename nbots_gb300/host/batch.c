@@ -20,7 +20,7 @@
 #include <stdlib.h>
 #include <string.h>
 
-#include "nbots_gb300.h"
+#include "fem_internal.h"
 
 struct nbg_batch {
 	uint32_t n;
@@ -242,18 +242,16 @@ int nbg_batch_assemble_simp(nbg_batch_t *b, const double *rho, double nu, double
 	if (!b || !rho)
 		return NBG_ERR_ARG;
 	const uint32_t Ne = b->m.N_elem;
-	double *E = malloc(8 * (size_t)(Ne ? Ne : 1));
-	if (!E)
-		return NBG_ERR_NOMEM;
-	for (uint32_t e = 0; e < Ne; e++)
-		E[e] = Emin + pow(rho[e], penal) * (E0 - Emin);
+	/* the moduli on the device, as nbg_fem_simp computes them */
+	TRY(nbg_h2d(b->d_rho, rho, 8 * (size_t)Ne, b->stream));
+	TRY(nbg_simp_modulus_f64(Ne, b->d_rho, penal, E0, Emin,
+				 nbg_fem_device_ptr(b->f, NBG_FEM_E), b->stream));
 	const double g0[2] = {0.0, 0.0};
-	rc = nbg_fem_assemble(b->f, E, nu, thickness, 0.0, 0, g0, NULL);
+	rc = nbg_fem_assemble_dev_damage(b->f, NULL, nu, thickness, 0.0, 0, g0, NULL, NULL);
 	if (rc != NBG_OK)
 		goto fail;
 	TRY(nbg_fem_apply_bcs(b->f, &b->bcs, 1.0));
 	TRY(nbg_fem_block_layout(b->f, NULL));
-	TRY(nbg_h2d(b->d_rho, rho, 8 * (size_t)Ne, b->stream));
 	TRY(nbg_stream_sync(b->stream));
 	b->nu = nu;
 	b->thickness = thickness;
@@ -267,7 +265,6 @@ int nbg_batch_assemble_simp(nbg_batch_t *b, const double *rho, double nu, double
 						     nbg_fem_device_ptr(b->f, NBG_FEM_CONN), nu,
 						     thickness, b->d_rho, penal, E0, Emin, b->d_dJ));
 fail:
-	free(E);
 	return rc;
 }
 
