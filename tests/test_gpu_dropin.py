@@ -8,7 +8,6 @@ import pytest
 
 from conftest import GOLDEN_CASES, cg_iters_close, load_golden
 from kat import BEAM_MAX_DISP, PWH_MAX_VM_ERR, max_disp, pwh_mean_vm_error
-from oracle import oracle as O
 
 pytestmark = pytest.mark.gpu
 FEM_CASES = [c for c in GOLDEN_CASES if c != "q4_lognormal_32x16"]  # one material only

@@ -2,7 +2,6 @@
 oracle.  Integer and FP64 assembly/BC stages are bit-exact; the CG solve
 differs from nbots' serial sums only in its reduction order, so the
 displacements must agree within 1e-10 relative L2."""
-import ctypes as C
 
 import numpy as np
 import pytest
