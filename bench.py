@@ -16,10 +16,10 @@ of the solver kernel and a CPU baseline.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
 
-With --impl reference the oracle's C restatement of nbots' Jacobi-PCG runs on
-the host cores (OpenMP, all threads) on a bounded sample of iterations per
-step, projected to the iteration count nbots' algorithm needs on this
-workload.
+With --impl reference nbots' own Jacobi-PCG (cg_precond_jacobi.c:13-90)
+runs on the host cores (OpenMP, all threads) to convergence in every step:
+the library built from the nbots sources (oracle/_ref) where it exists on
+the machine, else the oracle's C restatement of the same loop.
 """
 from __future__ import annotations
 
@@ -41,12 +41,6 @@ METRIC = "FP64 vs mixed-prec time-to-1e-8 relres at 1M DOF (s); SpMV HBM GB/s vs
 WORKLOAD = ("C2: 1024x512 Q4 cantilever, 1,051,650 dof, lognormal E (sigma 0.5, seed 2), "
             "clamped left edge, point load + top traction 0.01; Jacobi-PCG to relres 1e-8 from u=0")
 TOL = 1e-8
-# Jacobi-PCG iterations nbots' own algorithm (cg_precond_jacobi.c, FP64, one
-# thread) needs on this workload to reach ||g|| <= 1e-8 ||F||: measured by
-# running the oracle restatement to convergence (7017 on the GPU copy of the
-# same iteration).  Used to project the bounded CPU samples.
-NBOTS_ITERS_C2 = 7017
-CPU_SAMPLE_ITERS = 60
 
 
 def peaks():
@@ -105,24 +99,86 @@ class Clocks:
 
 
 # ------------------------------------------------------------------ CPU
-def cpu_baseline(p, threads=None, iters=CPU_SAMPLE_ITERS):
-    """The oracle's restatement of nbots' Jacobi-PCG on the host cores: a
-    bounded run of `iters` iterations, projected to NBOTS_ITERS_C2."""
-    from oracle import oracle as O
-    threads = threads or os.cpu_count() or 1
-    fl = O.Flat(p)
-    rp, ci = O.pattern(fl)
-    _, K, F = O.assemble(fl, rp, ci)
-    O.set_bconditions(fl, rp, ci, K, F)
-    O.cg_jacobi(rp, ci, K, F, max_iter=2, tol=0.0, threads=threads)  # warm the threads
-    t0 = O.wtime()
-    O.cg_jacobi(rp, ci, K, F, max_iter=iters, tol=0.0, threads=threads)
-    dt = O.wtime() - t0
-    per_it = dt / iters
-    return {"value": per_it * NBOTS_ITERS_C2, "unit": "s", "cores": threads, "kind": "port",
-            "sample": f"{iters} Jacobi-PCG iterations of the C oracle (OpenMP, {threads} "
-                      f"threads) on the full workload, {per_it * 1e3:.2f} ms/iteration, "
-                      f"projected to {NBOTS_ITERS_C2} iterations"}
+def cpu_model():
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.startswith("Model name:"):
+                return line.split(":", 1)[1].strip()
+    except Exception:
+        pass
+    import platform
+    return platform.processor() or platform.machine()
+
+
+class CpuSystem:
+    """The C2 system (K and F after boundary conditions) on the host, built by
+    the oracle (setup, not timed), with nbots' own SpMV and Jacobi-PCG from
+    the library built from its sources when it loads here, else the oracle's
+    C restatement of the same loops."""
+
+    def __init__(self, p, threads=None):
+        from oracle import oracle as O
+        from oracle import ref_cpu as R
+        self.O, self.R = O, R
+        self.threads = threads or os.cpu_count() or 1
+        fl = O.Flat(p)
+        self.rp, self.ci = O.pattern(fl)
+        _, self.K, self.F = O.assemble(fl, self.rp, self.ci)
+        O.set_bconditions(fl, self.rp, self.ci, self.K, self.F)
+        self.tol = TOL * float(np.linalg.norm(self.F))  # nbots' tolerance is absolute
+        self.kind = "reference" if R.available() else "port"
+        self.m = R.Matrix(self.rp, self.ci, self.K) if self.kind == "reference" else None
+
+    def what(self):
+        return ("nbots' own code (oracle/_ref/libnbots_ref.so, built from the nbots sources)"
+                if self.kind == "reference" else
+                "the oracle's C restatement of nbots' loops (nbots_oracle.c)")
+
+    def spmv(self, x):
+        if self.m is not None:
+            return self.R.spmv(self.m, x, self.threads)
+        return self.O.spmv(self.rp, self.ci, self.K, x, self.threads)
+
+    def cg(self, max_iter=None):
+        """One Jacobi-PCG from x = 0 with nbots' absolute tolerance
+        1e-8 ||F||: (seconds, iterations, status)."""
+        t0 = time.perf_counter()
+        if self.m is not None:
+            _, it, _, st = self.R.cg_jacobi(self.m, self.F, self.tol, self.threads,
+                                            max_iter=max_iter)
+        else:
+            _, it, _, st = self.O.cg_jacobi(self.rp, self.ci, self.K, self.F,
+                                            max_iter=max_iter, tol=self.tol,
+                                            threads=self.threads)
+        return time.perf_counter() - t0, it, st
+
+    def spmv_median(self, reps=7):
+        x = np.random.default_rng(7).standard_normal(self.F.shape[0])
+        self.spmv(x)
+        ts = []
+        for _ in range(reps):
+            t0 = time.perf_counter()
+            self.spmv(x)
+            ts.append(time.perf_counter() - t0)
+        return float(np.median(ts))
+
+
+def cpu_baseline(p):
+    """nbots' Jacobi-PCG run to convergence once on the full workload on the
+    host cores, and the median of 7 SpMVs (sparse.c:405-414)."""
+    cs = CpuSystem(p)
+    cs.cg(max_iter=20)  # threads and pages warm
+    t_cg, it, st = cs.cg()
+    t_spmv = cs.spmv_median()
+    nnz, N = cs.ci.shape[0], cs.F.shape[0]
+    b_spmv = 12 * nnz + 4 * (N + 1) + 16 * N
+    return {"value": t_cg, "unit": "s", "cores": cs.threads, "kind": cs.kind,
+            "cpu": cpu_model(), "iters": it, "status": st,
+            "spmv_ms_median_of_7": t_spmv * 1e3, "spmv_gbs": b_spmv / t_spmv / 1e9,
+            "sample": f"one full Jacobi-PCG solve to ||g|| <= 1e-8 ||F|| from u = 0 ({it} "
+                      f"iterations) with {cs.what()}, OpenMP {cs.threads} threads; SpMV: "
+                      f"median of 7"}
 
 
 def run_reference(args):
@@ -131,12 +187,19 @@ def run_reference(args):
         return 0
     from nbots_gb300 import workloads as W
     p = W.config_c2()
+    cs = CpuSystem(p)
+    # warm-up steps: bounded solves (threads, pages and caches warm); each
+    # timed step is one full solve to the tolerance
     for _ in range(args.warmup):
-        cpu_baseline(p, iters=10)
-    vals = [cpu_baseline(p) for _ in range(args.steps)]
-    v = float(np.median([x["value"] for x in vals]))
-    cb = dict(vals[0])
-    cb["value"] = v
+        cs.cg(max_iter=50)
+    runs = [cs.cg() for _ in range(args.steps)]
+    ts = [r[0] for r in runs]
+    v = float(np.median(ts))
+    cb = {"value": v, "unit": "s", "cores": cs.threads, "kind": cs.kind, "cpu": cpu_model(),
+          "iters": runs[0][1], "status": runs[0][2], "s_min_max": [min(ts), max(ts)],
+          "sample": f"every step one full Jacobi-PCG solve to ||g|| <= 1e-8 ||F|| from u = 0 "
+                    f"({runs[0][1]} iterations) with {cs.what()}, OpenMP {cs.threads} "
+                    f"threads; warm-up steps: 50 iterations each"}
     line = {"metric": METRIC, "value": v, "unit": "s", "n_gpus": args.gpus, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": v * 1e3, "higher_is_better": False,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -243,12 +306,14 @@ def bench_damage(L, W, with_cpu):
     return out
 
 
-def bench_fem_entry(W):
+def bench_fem_entry(W, with_cpu):
     """nbots' FEM entry through the drop-in symbol (nb_fem_compute_2D_Solid_
     Mechanics with nbots' objects built by the host library): the 1024x512
     cantilever with one material (E = 1, the entry takes one), host arrays in
-    and out, pattern, assembly, boundary conditions, nbots-order Jacobi-PCG
-    (x0 = 0, max_iter = N, absolute 1e-8) and strain, wall time."""
+    and out, pattern, assembly, boundary conditions, nbots' Jacobi-PCG
+    iteration (x0 = 0, max_iter = N, absolute 1e-8) and strain, wall time.
+    Beside it the same entry on the host as nbots ships it, one thread
+    (static_elasticity2D.c:88-90), on the oracle's restatement of each stage."""
     from nbots_gb300.dropin import NbotsObjects
     warm = NbotsObjects(W.cantilever_q4(16, 8))
     warm.fem()
@@ -260,11 +325,82 @@ def bench_fem_entry(W):
     st, u, strain = ob.fem()
     t = time.perf_counter() - t0
     ob.close()
-    return {"workload": "C2 mesh and loads, one material E = 1", "status": int(st),
-            "s_per_call": t, "max_abs_u": float(np.max(np.abs(u)))}
+    out = {"workload": "C2 mesh and loads, one material E = 1", "status": int(st),
+           "s_per_call": t, "max_abs_u": float(np.max(np.abs(u)))}
+    if with_cpu:
+        from oracle import oracle as O
+        t0 = time.perf_counter()
+        ref = O.fem(p, threads=1)
+        t_cpu = time.perf_counter() - t0
+        out["cpu_one_thread"] = {
+            "s_per_call": t_cpu, "kind": "port", "cores": 1, "cg_iters": ref["cg_niter"],
+            "u_rel_diff_vs_dropin": float(np.linalg.norm(u - ref["u"]) /
+                                          np.linalg.norm(ref["u"])),
+            "sample": "one call: pattern, assembly, boundary conditions, Jacobi-PCG to "
+                      "absolute 1e-8, strain, on the oracle's C restatement, one thread"}
+        out["speedup_vs_cpu_one_thread"] = t_cpu / t
+    return out
 
 
-def bench_c5(args, lib, L, W, sp, dev, stream, flush):
+def bench_dropin_sparse(W, cpu_spmv_s=None):
+    """nb_sparse_multiply_vector and nb_sparse_solve_CG_precond_Jacobi called
+    as nbots calls them: an nb_sparse_t from nb_sparse_create holding K after
+    boundary conditions of the C2 system, host vectors in and out.  The first
+    call on the matrix builds its device copy; later calls on the unchanged
+    matrix send only the vectors.  After one nb_sparse_add the next call
+    re-sends the values."""
+    from nbots_gb300.dropin import libs, sparse_from_csr
+    from oracle import oracle as O
+    G, _ = libs()
+    p = W.config_c2()
+    fl = O.Flat(p)
+    rp, ci = O.pattern(fl)
+    _, K, F = O.assemble(fl, rp, ci)
+    O.set_bconditions(fl, rp, ci, K, F)
+    A, keep = sparse_from_csr(p, K)
+    N = p.n_dof
+    x = np.random.default_rng(11).standard_normal(N)
+    y = np.zeros(N)
+
+    def spmv():
+        t0 = time.perf_counter()
+        G.nb_sparse_multiply_vector(A, x.ctypes.data, y.ctypes.data, 1)
+        return time.perf_counter() - t0
+    t_first = spmv()
+    ts = [spmv() for _ in range(7)]
+    exact = bool(np.array_equal(y.view(np.uint64), O.spmv(rp, ci, K, x, 8).view(np.uint64)))
+    r0 = A.contents.rows_values[0][0]
+    G.nb_sparse_add(A, 0, int(ci[0]), 0.0)  # a write: the next call re-sends the values
+    t_dirty = spmv()
+    G.nb_sparse_set(A, 0, int(ci[0]), r0)
+    tol = TOL * float(np.linalg.norm(F))
+    it, tr = C.c_uint32(0), C.c_double(0)
+
+    def cg():
+        u = np.zeros(N)
+        t0 = time.perf_counter()
+        st = G.nb_sparse_solve_CG_precond_Jacobi(A, F.ctypes.data, u.ctypes.data, N, tol,
+                                                  C.byref(it), C.byref(tr), 1)
+        return time.perf_counter() - t0, st, u
+    t_cg_first, _, _ = cg()
+    t_cg, st, u = cg()
+    relres = float(np.linalg.norm(F - O.spmv(rp, ci, K, u, 8)) / np.linalg.norm(F))
+    G.nb_sparse_destroy(A)
+    t_spmv = float(np.median(ts))
+    out = {"workload": "C2 K and F after boundary conditions in an nb_sparse_t, host vectors",
+           "spmv": {"s_first_call": t_first, "s_median_of_7": t_spmv,
+                    "s_after_one_write": t_dirty, "bit_exact": exact,
+                    "h2d_bytes": 8 * N, "d2h_bytes": 8 * N},
+           "cg_jacobi": {"s_first_call": t_cg_first, "s_per_call": t_cg, "status": int(st),
+                         "iters": it.value, "relres_fp64": relres,
+                         "h2d_bytes": 16 * N, "d2h_bytes": 8 * N,
+                         "stop": "nbots' (absolute 1e-8 ||F||, lagged test)"}}
+    if cpu_spmv_s:
+        out["spmv"]["speedup_vs_cpu_spmv"] = cpu_spmv_s / t_spmv
+    return out
+
+
+def bench_c5(args, lib, L, W, sp, dev, stream, flush, share=None):
     """96 batched SIMP cantilevers: one graph launch = zero u, batched mixed
     CG to relres 1e-8 per instance, compliance sensitivities.  Per-instance
     errors against an FP64 solve of the same merged system to relres 1e-13."""
@@ -272,6 +408,9 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush):
     from nbots_gb300.batch import Batch
     t0 = time.perf_counter()
     probs = W.config_c5()
+    n_all = len(probs)
+    if share is not None:  # this rank's instances
+        probs = [probs[k] for k in share]
     b = Batch(probs, stream=sp)
     rho = [p.meta["rho"] for p in probs]
     b.assemble_simp(rho, nu=probs[0].nu, thickness=probs[0].thickness)
@@ -293,6 +432,8 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush):
         e1.synchronize()
         ts.append(e0.elapsed_time(e1) / 1e3)
     res, J = b.results()
+    from nbots_gb300 import replicas as R
+    t_all = R.max_over_ranks([float(np.median(ts))], device=dev)[0]  # the slowest share
     us = b.displacements()
     dJ = b.sensitivities()
     t = float(np.median(ts))
@@ -331,9 +472,12 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush):
     out = {"workload": "C5: 96 Q4 SIMP cantilevers, sizes U{64x32,128x64,256x128,512x256} "
                        "seed 5, rho~U(0.2,1.0), 1-4 point loads; mixed CG to relres 1e-8 per "
                        "instance + compliance gradients, one CUDA graph launch",
-           "instances": len(probs), "dof_total": int(sum(p.n_dof for p in probs)),
-           "dof_merged_padded": N, "s_per_batch": t, "solves_per_s": len(probs) / t,
-           "dof_iters_per_s": float(sum(p.n_dof * r.niter for p, r in zip(probs, res))) / t,
+           "instances": n_all, "instances_rank0": len(probs),
+           "dof_total_rank0": int(sum(p.n_dof for p in probs)),
+           "dof_merged_padded_rank0": N, "s_per_batch": t_all, "solves_per_s": n_all / t_all,
+           "ranks_sharing_the_batch": R.world()[1],
+           "dof_iters_per_s_rank0": float(sum(p.n_dof * r.niter for p, r in zip(probs, res)))
+                                    / t,
            "status_all_zero": all(r.status == 0 for r in res),
            "iters_min_max": [min(iters), max(iters)],
            "max_relres": max(r.relres for r in res),
@@ -349,13 +493,14 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush):
     return out
 
 
-def run_c3(args):
+def bench_c3(args, with_cpu):
     """The unstructured T3 L-shape (2M seeded points, about 4M dof): mesh
     generation (host, not timed), pattern + upload, assembly + boundary
     conditions, then mixed-precision and fast FP64 Jacobi-PCG to relres 1e-8
     from u = 0 (CUDA events, L2 flushed before each solve), the mixed
-    solution's distance from the FP64 one, and a bounded sample of the
-    oracle's CPU iteration projected to the FP64 iteration count."""
+    solution's distance from the FP64 one, and nbots' CPU iteration on the
+    host cores timed over 200 iterations (per iteration beside the GPU's;
+    a full CPU solve takes about two minutes)."""
     import torch
     from nbots_gb300 import _lib as L
     from nbots_gb300 import workloads as W
@@ -456,21 +601,17 @@ def run_c3(args):
     bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 24 * N + 136 * (N // 2)
     hbm, peak_kind = peaks()
     cpu = None
-    if not args.no_cpu_baseline:
-        from oracle import oracle as O
-        threads = os.cpu_count() or 1
-        fl = O.Flat(p)
-        rp, ci = O.pattern(fl)
-        _, K, Fc = O.assemble(fl, rp, ci)
-        O.set_bconditions(fl, rp, ci, K, Fc)
-        O.cg_jacobi(rp, ci, K, Fc, max_iter=2, tol=0.0, threads=threads)
-        c0 = O.wtime()
-        O.cg_jacobi(rp, ci, K, Fc, max_iter=20, tol=0.0, threads=threads)
-        per_it = (O.wtime() - c0) / 20
-        cpu = {"value": per_it * r_fp64.niter, "unit": "s", "cores": threads, "kind": "port",
-               "sample": f"20 Jacobi-PCG iterations of the C oracle ({threads} threads), "
-                         f"{per_it * 1e3:.1f} ms/iteration, projected to the FP64 GPU "
-                         f"iteration count {r_fp64.niter}"}
+    if with_cpu:
+        cs = CpuSystem(p)
+        cs.cg(max_iter=10)
+        t_it, n_it, _ = cs.cg(max_iter=200)
+        per_it = t_it / max(n_it, 1)
+        cpu = {"ms_per_iteration": per_it * 1e3, "cores": cs.threads, "kind": cs.kind,
+               "iterations_timed": n_it,
+               "gpu_fp64_ms_per_iteration": t_fp64 / r_fp64.niter * 1e3,
+               "per_iteration_speedup_fp64_gpu": per_it / (t_fp64 / r_fp64.niter),
+               "sample": f"{n_it} Jacobi-PCG iterations with {cs.what()}, OpenMP "
+                         f"{cs.threads} threads, timed (no projection to a full solve)"}
     line = {"workload": "C3: T3 L-shape [0,2]^2 minus (1,2]^2, 2M seeded uniform points + "
                         "boundary points, Delaunay, Z-order numbering; E=1, nu=0.25, bottom "
                         "clamped, unit +x traction on x=1, y in [1,2]; Jacobi-PCG to relres "
@@ -495,9 +636,13 @@ def run_c3(args):
                          "relres_fp64": relres(u_fp64)},
             "speedup_mixed_vs_fp64_gpu": t_fp64 / t_mixed,
             "dof_iters_per_s_mixed": N * r_mixed.niter / t_mixed,
-            "peak_gbs": hbm, "peak_kind": peak_kind, "cpu_baseline": cpu}
-    print(json.dumps(line))
+            "peak_gbs": hbm, "peak_kind": peak_kind, "cpu": cpu}
     s.close()
+    return line
+
+
+def run_c3(args):
+    print(json.dumps(bench_c3(args, not args.no_cpu_baseline)))
     return 0
 
 
@@ -613,6 +758,20 @@ def run_gpu(args):
         assert rc == 0, rc
         return r
     t_exact, r_exact = timed(nbots_gpu, 1, 0)
+
+    # nbots' iteration and stop test on the block layout with FMAs: the
+    # drop-in nb_sparse_solve_CG_precond_Jacobi's solver (absolute tolerance
+    # 1e-8 ||F||, as nbots takes it)
+    Fnorm = float(np.linalg.norm(s.get(L.FEM_F)))
+
+    def nbots_block():
+        r = L.CgResult()
+        rc = lib.nbg_cg_bsr_f64(C.byref(A), F, u.data_ptr(), 4 * N, TOL * Fnorm,
+                                L.CG_JACOBI | L.CG_NBOTS_STOP, C.byref(r), ws.data_ptr(),
+                                ws_bytes, sp)
+        assert rc == 0, rc
+        return r
+    t_nblk, r_nblk = timed(nbots_block, 2, 1)
 
     # ---- accuracy: true FP64 residuals and displacement differences
     Ft = torch.from_numpy(s.get(L.FEM_F)).to(dev)
@@ -757,14 +916,22 @@ def run_gpu(args):
     # ---- max over ranks
     t_all, e2e_all = R.max_over_ranks([t_med, e2e_v], device=dev)
 
-    fem_entry = None if args.no_c4 else bench_fem_entry(W)
-    c4 = None if args.no_c4 else bench_c4(lib, L, W)
-    c5 = None if args.no_c5 else bench_c5(args, lib, L, W, sp, dev, stream, flush)
-    dmg = None if args.no_damage else bench_damage(L, W, rank == 0 and not args.no_cpu_baseline)
+    # the other workloads and the CPU legs run on one GPU only; with several
+    # ranks each solves its own share of the batched instances
+    single = world == 1
+    with_cpu = rank == 0 and single and not args.no_cpu_baseline
+    cpu = cpu_baseline(p) if with_cpu else None
+    dropin = None
+    if single and not args.no_dropin:
+        dropin = bench_dropin_sparse(W, cpu["spmv_ms_median_of_7"] / 1e3 if cpu else None)
+    fem_entry = bench_fem_entry(W, with_cpu) if single and not args.no_c4 else None
+    c4 = bench_c4(lib, L, W) if single and not args.no_c4 else None
+    c5 = None if args.no_c5 else bench_c5(args, lib, L, W, sp, dev, stream, flush,
+                                          R.shard(96, rank, world))
+    dmg = bench_damage(L, W, with_cpu) if single and not args.no_damage else None
+    s.close()
+    c3 = bench_c3(args, with_cpu) if single and not args.no_c3 else None
 
-    cpu = None
-    if rank == 0 and not args.no_cpu_baseline:
-        cpu = cpu_baseline(p)
     if rank == 0:
         line = {
             "metric": METRIC, "value": t_all, "unit": "s", "n_gpus": world,
@@ -785,12 +952,17 @@ def run_gpu(args):
                          "achieved_gbs": fp64_bytes_iter * r_fp64.niter /
                                          float(np.median(t_fp64)) / 1e9,
                          "bound": "fp64 issue (about 2 FP64 FMA per clock per SM on GB300)"},
-            "nbots_order_fp64_gpu": {"s_per_solve": float(t_exact[0]), "iters": r_exact.niter},
+            "nbots_order_fp64_gpu": {"s_per_solve": float(t_exact[0]), "iters": r_exact.niter,
+                                     "what": "nbots' arithmetic operation for operation on "
+                                             "the CSR (k_cg_f64; NBG_DROPIN_EXACT_CG=1)"},
+            "nbots_iteration_block_fp64_gpu": {
+                "s_per_solve": float(np.median(t_nblk)), "iters": r_nblk.niter,
+                "what": "nbots' iteration and lagged stop test on the block layout with FMAs "
+                        "(k_cg_bsr_f64, NBG_CG_NBOTS_STOP): the drop-in CG's solver"},
             "speedup_mixed_vs_fp64_gpu": float(np.median(t_fp64)) / t_all,
-            "speedup_mixed_vs_plain_fp64_gpu": float(t_exact[0]) / t_all,
-            "speedup_note": "plain = the FP64 GPU path that matches nbots (CSR, nbots' "
-                            "arithmetic and iteration, the drop-in's solver); fp64 = the "
-                            "tuned FP64 block-layout CG",
+            "speedup_mixed_vs_nbots_order_fp64_gpu": float(t_exact[0]) / t_all,
+            "speedup_note": "fp64 = the tuned FP64 block-layout CG (the headline comparison); "
+                            "nbots_order = nbots' arithmetic on the CSR",
             "setup_s": {"pattern_and_upload": t_create, "first_call": t_create_first,
                         "host_pattern_and_incidence": t_host_pattern,
                         "assembly_and_bcs": t_asm},
@@ -807,7 +979,9 @@ def run_gpu(args):
                     "d2h_bytes_per_step": int(8 * N),
                     "path": "nbg_solver_set_matrix (values, pattern kept) + nbg_solver_solve "
                             "(mixed) from pinned host buffers"},
+            "dropin_sparse": dropin,
             "fem_entry_dropin": fem_entry,
+            "c3_lshape": c3,
             "c4_simp": c4,
             "c5_batch": c5,
             "damage": dmg,
@@ -818,7 +992,6 @@ def run_gpu(args):
         }
         print(json.dumps(line))
     R.finalize()
-    s.close()
     return 0
 
 
@@ -912,8 +1085,12 @@ def main():
     ap.add_argument("--no-c4", action="store_true", help="skip the SIMP gradient timings")
     ap.add_argument("--no-c5", action="store_true", help="skip the batched solves")
     ap.add_argument("--no-damage", action="store_true", help="skip the damage-solve timings")
+    ap.add_argument("--no-dropin", action="store_true",
+                    help="skip the nb_sparse_* drop-in timings")
+    ap.add_argument("--no-c3", action="store_true",
+                    help="skip the 4M-dof T3 L-shape (its mesh takes about a minute)")
     ap.add_argument("--c3", action="store_true",
-                    help="run the 4M-dof unstructured T3 L-shape instead (mesh generation "
+                    help="run only the 4M-dof unstructured T3 L-shape (mesh generation "
                          "takes about a minute on the host)")
     ap.add_argument("--profile", choices=["mixed", "fp64", "spmv", "damage", "pattern", "nbots"],
                     help="one bounded kernel launch for ncu instead of the benchmark")

@@ -96,12 +96,39 @@ void nb_sparse_multiply_vector(const nb_sparse_t *A, const double *in, double *o
 /* sparse.h:58-59, sparse.c:416-430 (host side, same order) */
 void nb_sparse_set_Dirichlet_condition(nb_sparse_t *A, double *RHS, uint32_t idx,
 				       double value);
+/* The remaining writers of sparse.h (sparse.c:148-162, 221-227, 289-347,
+ * 394-403), replaced so that the drop-in sees every write to a matrix it
+ * keeps a device copy of.  The first four run here; transpose,
+ * get_transpose and fill_permutation forward to the next definition in link
+ * order (nbots' own) and record NBG_ERR_ARG when there is none. */
+void nb_sparse_set_identity_row(nb_sparse_t *A, uint32_t row);
+void nb_sparse_make_diagonal(nb_sparse_t *A, double diag_val);
+void nb_sparse_scale(nb_sparse_t *A, double factor);
+void nb_sparse_multiply_scalar(nb_sparse_t *A, double scalar, uint32_t omp_parallel_threads);
+void nb_sparse_transpose(nb_sparse_t *A);
+void nb_sparse_get_transpose(const nb_sparse_t *A, nb_sparse_t *At);
+void nb_sparse_fill_permutation(const nb_sparse_t *A, nb_sparse_t *Ar, const uint32_t *perm,
+				const uint32_t *iperm);
+
+/* Device copies.  A matrix made by nb_sparse_create / nb_sparse_clone keeps
+ * its pattern, values and block layout on the GPU from one
+ * nb_sparse_multiply_vector / nb_sparse_solve_* call to the next; the
+ * functions above mark it changed, so the next GPU call re-sends the values
+ * (the pattern never changes), and nb_sparse_destroy frees the copy.  Code
+ * that writes rows_values directly calls nbg_dropin_sparse_touch(A) before
+ * the next GPU call.  NBG_DROPIN_CACHE_MB (default 16384) bounds the device
+ * memory of all copies (least recently used dropped first; 0: no copies).
+ * Matrices nbots allocated itself are sent whole on every call. */
+void nbg_dropin_sparse_touch(const nb_sparse_t *A);
 
 /* ------------------------------------------------------- replaced: solvers */
 /* headers/nb/solver_bot/sparse/solvers/cg_precond_jacobi.h:8-15,
  * cg_precond_jacobi.c:13-90: nbots' iteration (g = Ax - b, absolute tolerance,
- * lagged stop test) in one persistent GPU kernel.  Returns 0 or 1 (tolerance
- * not reached) like nbots, or a negative nbg status on a GPU error. */
+ * lagged stop test) in one persistent GPU kernel, on the 2x2-block layout
+ * with FMAs when the pattern is node-blocked (nb_sparse_create(.., 2)), else
+ * on the CSR with nbots' arithmetic; NBG_DROPIN_EXACT_CG=1 selects the CSR
+ * form always.  Returns 0 or 1 (tolerance not reached) like nbots, or a
+ * negative nbg status on a GPU error. */
 int nb_sparse_solve_CG_precond_Jacobi(const nb_sparse_t *A, const double *b, double *x,
 				      uint32_t max_iter, double tolerance,
 				      uint32_t *niter_performed, double *tolerance_reached,

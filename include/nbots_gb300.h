@@ -175,6 +175,10 @@ int nbg_spmv_csr_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_id
 /* --------------------------------------------------------------------- CG */
 #define NBG_CG_JACOBI 1u     /* Jacobi preconditioner (else plain CG) */
 #define NBG_CG_RELATIVE 2u   /* stop on ||g|| <= tol ||b|| (else absolute, nbots) */
+/* nbg_cg_bsr_f64 only: nbots' stop rule (cg_precond_jacobi.c:45, 80-89), the
+ * lagged ||g|| of the previous iteration, reported as tol_reached (else the
+ * current ||g||, confirmed on the true residual b - A x) */
+#define NBG_CG_NBOTS_STOP 4u
 
 typedef struct {
     uint32_t niter;       /* iterations performed */
@@ -200,10 +204,12 @@ int nbg_cg_f64(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
  * cudaMalloc / cudaFree).  No counterpart in nbots.  The scratch lives in a
  * 16 MiB file-scope device array that every GPU loading this library holds
  * until exit, so N is limited to 345,408 dofs (larger N: NBG_ERR_ARG, with
- * the reason in nbg_last_error).  The first call on a device looks up the
- * array's address with that device current; make it before any stream
- * capture.  All calls share the array: calls that overlap on the GPU race
- * and must be serialised by the caller. */
+ * the reason in nbg_last_error).  Every call looks up the array's device
+ * address on the current device (cudaGetSymbolAddress, no allocation), so a
+ * cudaDeviceReset between calls is safe; the first call on a device loads
+ * the library's kernels there: make it before any stream capture.  All calls
+ * share the array: calls that overlap on the GPU race and must be
+ * serialised by the caller. */
 int nbg_cg_f64_noalloc(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_idx,
                        const double *val, const double *b, double *x, uint32_t max_iter,
                        double tol, unsigned flags, nbg_cg_result_t *result, void *stream);
@@ -256,9 +262,15 @@ int nbg_bsr_fill(const nbg_bsr_t *A, const uint32_t *row_ptr, const uint32_t *co
 int nbg_spmv_bsr_f64(const nbg_bsr_t *A, const double *x, double *y, void *stream);
 int nbg_spmv_bsr_f32(const nbg_bsr_t *A, const float *x, float *y, void *stream);
 
-/* Fast persistent FP64 Jacobi-PCG on the block layout: FMA arithmetic,
- * reciprocal diagonal, stop on the current ||g|| (not nbots' lagged one);
- * NBG_CG_RELATIVE selects ||g|| <= tol ||b||.  x holds x0 on entry. */
+/* Fast persistent FP64 CG on the 2x2-block SELL layout (Jacobi with
+ * NBG_CG_JACOBI, else plain): FMA arithmetic, reciprocal diagonal.  Default
+ * stop: the current ||g|| meets the target and the true residual b - A x,
+ * recomputed in FP64 at that point, meets it too (else that residual
+ * replaces the recurrence's and the iteration goes on); tol_reached is then
+ * the true residual norm.  With NBG_CG_NBOTS_STOP: nbots' iteration and stop
+ * test (the lagged ||g||, one iteration past the first ||g|| <= tol),
+ * iterates within rounding of nbots' own.  NBG_CG_RELATIVE selects
+ * ||g|| <= tol ||b||.  x holds x0 on entry. */
 size_t nbg_cg_bsr_workspace_bytes(uint32_t N);
 int nbg_cg_bsr_f64(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_iter,
                    double tol, unsigned flags, nbg_cg_result_t *result, void *ws,
@@ -333,6 +345,8 @@ int nbg_mixed_batch_tune(nbg_mixed_batch_t *m, uint32_t n_cand, const double *ga
 #define NBG_METHOD_NBOTS 0   /* nbots' iteration in FP64 (nbg_cg_f64) */
 #define NBG_METHOD_FP64 1    /* fast FP64 on the block layout (nbg_cg_bsr_f64) */
 #define NBG_METHOD_MIXED 2   /* mixed precision, FP64 reliable updates (nbg_cg_mixed) */
+#define NBG_METHOD_NBOTS_FAST 3  /* nbots' iteration and stop test on the block layout
+                                  * (nbg_cg_bsr_f64 with NBG_CG_NBOTS_STOP) */
 #define NBG_PATTERN_SAME 1u  /* same pattern as the previous call: send values only */
 #define NBG_CSR_ONLY 2u      /* skip the block layout (only NBG_METHOD_NBOTS will run) */
 
@@ -347,11 +361,26 @@ typedef struct {
 typedef struct nbg_solver nbg_solver_t;
 int nbg_solver_create(nbg_solver_t **out, void *stream);
 void nbg_solver_destroy(nbg_solver_t *s);
+/* val NULL: the pattern only; the device values are left for the caller to
+ * write (nbg_solver_device_csr, then nbg_solver_values_changed). */
 int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
                           const uint32_t *col_idx, const double *val, unsigned flags);
 /* x holds x0 on entry and the solution on return (host memory). */
 int nbg_solver_solve(nbg_solver_t *s, const double *b, double *x, uint32_t max_iter,
                      double tol, unsigned flags, int method, nbg_solve_info_t *info);
+
+/* y = A x with nbots' row sums (nbg_spmv_csr_f64, bit-exact) on the
+ * solver's matrix; in and out in host memory. */
+int nbg_solver_multiply(nbg_solver_t *s, const double *in, double *out);
+/* Device pointers of the solver's CSR (valid until the next set_matrix with a
+ * new pattern or destroy); any output may be NULL.  A caller that writes
+ * new values into *val on the device calls nbg_solver_values_changed so the
+ * block layout follows. */
+int nbg_solver_device_csr(nbg_solver_t *s, const uint32_t **row_ptr, const uint32_t **col_idx,
+                          double **val);
+int nbg_solver_values_changed(nbg_solver_t *s);
+/* Device bytes the solver holds (matrix, block layout, vectors, workspace). */
+size_t nbg_solver_device_bytes(const nbg_solver_t *s);
 
 /* Page-locked host memory (for asynchronous copies). */
 int nbg_host_alloc(void **ptr, size_t bytes);
@@ -474,10 +503,11 @@ typedef struct {
  * `logfile` (NULL: no log).  Displacements end in NBG_FEM_U, damage in
  * NBG_FEM_DAMAGE, strain in NBG_FEM_STRAIN.  Returns 0, NBG_DISTORTED, or an
  * error; Gauss-Seidel stops with NBG_ERR_TIMEOUT after 600 s.  method: the
- * inner solver, NBG_METHOD_NBOTS (nbots' iteration on the CSR, the drop-in's
- * choice) or NBG_METHOD_FP64 (the fast FP64 CG on the block layout, refilled
- * after every assembly; it stops on the current residual norm instead of
- * nbots' lagged one). */
+ * inner solver, NBG_METHOD_NBOTS (nbots' arithmetic and iteration on the
+ * CSR), NBG_METHOD_NBOTS_FAST (nbots' iteration and stop test on the block
+ * layout, refilled after every assembly; the drop-in's choice) or
+ * NBG_METHOD_FP64 (the fast FP64 CG on the block layout, stopping on the
+ * current residual norm, confirmed on the true residual). */
 int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, double thickness,
                    double density, int self_weight, const double gravity[2], double ft,
                    double gf, uint32_t n_steps, uint32_t max_iter, uint32_t max_iter_noenh,

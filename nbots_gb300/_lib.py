@@ -183,9 +183,9 @@ SIGS = {
 
 (FEM_ROW_PTR, FEM_COL_IDX, FEM_K, FEM_F, FEM_U, FEM_STRAIN, FEM_STRESS, FEM_E, FEM_NOD,
  FEM_CONN, FEM_MAIN_STRESS, FEM_DAMAGE) = range(12)
-CG_JACOBI, CG_RELATIVE = 1, 2
+CG_JACOBI, CG_RELATIVE, CG_NBOTS_STOP = 1, 2, 4
 ORDER_AUTO, ORDER_MESH, ORDER_SIGMA = 0, 1, 2
-METHOD_NBOTS, METHOD_FP64, METHOD_MIXED = 0, 1, 2
+METHOD_NBOTS, METHOD_FP64, METHOD_MIXED, METHOD_NBOTS_FAST = 0, 1, 2, 3
 PATTERN_SAME = 1
 
 

@@ -24,7 +24,6 @@
 // run to run.
 #include <cstdint>
 #include <cstdio>
-#include <mutex>
 
 #include "persist.cuh"
 
@@ -357,9 +356,14 @@ extern "C" int nbg_cg_f64(uint32_t N, const uint32_t* row_ptr, const uint32_t* c
 //    this library, until the process exits; a system fits when
 //    nbg_cg_workspace_bytes(N) is at most that, i.e. N <= 345,408 dofs;
 //    larger N is rejected with NBG_ERR_ARG and a message in nbg_last_error;
-//  * the array's device address is looked up (cudaGetSymbolAddress) by the
-//    first call on each device, with that device current; make that first
-//    call before any stream capture;
+//  * in host code g_cg_scratch names a host-side shadow, not device memory,
+//    so every call looks up the array's device address on the current
+//    device (cudaGetSymbolAddress, which allocates nothing) and passes that
+//    to the kernel.  Looking it up per call rather than once per device keeps
+//    the address right after the host application resets the device
+//    (cudaDeviceReset), which gives the array a new address.  The first call
+//    on a device also loads this library's kernels there; make it before any
+//    stream capture;
 //  * every call shares the array and it keeps the last call's contents: each
 //    call clears the barrier, status and result words it needs at zero, and
 //    the work vectors are written before they are read;
@@ -367,10 +371,7 @@ extern "C" int nbg_cg_f64(uint32_t N, const uint32_t* row_ptr, const uint32_t* c
 //    device) race on the array and must be serialised by the caller.
 namespace {
 constexpr size_t kNoAllocScratchBytes = 16u << 20;
-constexpr int kNoAllocMaxDevices = 64;
 static __device__ __align__(256) unsigned char g_cg_scratch[kNoAllocScratchBytes];
-std::mutex g_noalloc_lock;
-void* g_noalloc_ptr[kNoAllocMaxDevices];
 }  // namespace
 
 extern "C" int nbg_cg_f64_noalloc(uint32_t N, const uint32_t* row_ptr, const uint32_t* col_idx,
@@ -386,19 +387,9 @@ extern "C" int nbg_cg_f64_noalloc(uint32_t N, const uint32_t* row_ptr, const uin
                       N, need, kNoAllocScratchBytes);
         return nbg_error_text(NBG_ERR_ARG, msg);
     }
-    int dev = 0;
-    NBG_CHECK(cudaGetDevice(&dev));
-    if (dev < 0 || dev >= kNoAllocMaxDevices) return NBG_ERR_ARG;
     void* ptr = nullptr;
-    {
-        std::lock_guard<std::mutex> g(g_noalloc_lock);
-        if (!g_noalloc_ptr[dev]) {
-            void* p = nullptr;
-            NBG_CHECK(cudaGetSymbolAddress(&p, g_cg_scratch));
-            g_noalloc_ptr[dev] = p;
-        }
-        ptr = g_noalloc_ptr[dev];
-    }
+    NBG_CHECK(cudaGetSymbolAddress(&ptr, g_cg_scratch));
+    if (ptr == nullptr) return nbg_error_text(NBG_ERR_CUDA, "nbg_cg_f64_noalloc: no address");
     return nbg_cg_f64(N, row_ptr, col_idx, val, b, x, max_iter, tol, flags, result, ptr,
                       kNoAllocScratchBytes, stream);
 }

@@ -1,6 +1,6 @@
-// Fast persistent FP64 Jacobi-PCG on the 2x2-block SELL layout (bsr.cu):
-// one cooperative launch per solve, one thread per node row, convergence
-// decided on the device, every spin bounded.
+// Fast persistent FP64 (Jacobi-preconditioned) CG on the 2x2-block SELL
+// layout (bsr.cu): one cooperative launch per solve, one thread per node
+// row, convergence decided on the device, every spin bounded.
 //
 // GB300 issues FP64 at a small fraction of its FP32 rate, so this kernel
 // keeps the FP64 instruction count at one FMA per stored value plus seven
@@ -9,7 +9,22 @@
 // recurrences to thread 0 and the cross-thread sums to warp 0, and uses
 // three barriers per iteration, one after each of L1 | L2 | L3 of
 // cg_precond_jacobi.c:50-74.
-// The stop test uses the current gradient norm, not nbots' lagged one.
+//
+// Two stop rules (template LAGGED):
+//  * nbots' (cg_precond_jacobi.c:45, 80-89; conjugate_gradient.c:40, 70-76):
+//    after iteration k the loop tests ||g_{k-1}||, the norm from before the
+//    iteration's update, against an absolute tolerance, so it runs one
+//    iteration past the first ||g|| <= tol, and reports that lagged norm.
+//    The drop-in nb_sparse_solve_* entries use it; with FMAs and the
+//    reciprocal diagonal the iterates differ from nbots' in the last bits
+//    only.
+//  * the fast rule: stop on the current ||g||, but only after confirming it
+//    on the true residual.  When the recurrence says converged, one extra
+//    pass recomputes g = A x - b (and q, g.q, g.g) from x; if the true norm
+//    is still above the target, g replaces the recurrence's residual and the
+//    iteration continues with beta from the true g.q (residual replacement),
+//    so the reported norm is always a true FP64 residual.
+// JAC = false is the unpreconditioned CG (q = g).
 #include <cstdint>
 
 #include "perm.cuh"
@@ -24,22 +39,28 @@ struct CgBsrArgs {
     const double* b;
     double* x;
     double *g, *q, *p, *w;
-    double* part;  // 6 * kMaxBlocks doubles: L1 [0,K), L2 [K,3K), init [3K,6K)
+    double* part;  // 6 * kMaxBlocks doubles: L1 [0,K), L2 [K,3K), init and check [3K,6K)
     unsigned* bar;
     int* status;
-    double* res;  // niter, status, gg, bb
+    double* res;  // niter, status, reported gg, bb, true-residual checks
     uint32_t max_iter;
     double tol;
     unsigned flags;
 };
 
+template <bool JAC>
+__device__ __forceinline__ double2 precond(double2 g, double2 di) {
+    return JAC ? make_double2(g.x * di.x, g.y * di.y) : g;
+}
+
+template <bool JAC, bool LAGGED>
 __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f64(CgBsrArgs a) {
     __shared__ double buf[3 * kPersistThreads];
     __shared__ double s_coef;  // alpha, then beta
-    __shared__ int s_stop;
+    __shared__ int s_stop;     // 0 iterate, 1 stop, 2 confirm on the true residual first
     __shared__ struct {
-        double gq, gg, bb, target2;
-        uint32_t k;
+        double gq, gq_old, gg, bb, target2, report;
+        uint32_t k, checks;
     } sc;  // scalar state, thread 0 only
     const unsigned G = gridDim.x;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -54,13 +75,17 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
     double2* __restrict__ w = reinterpret_cast<double2*>(a.w);
     const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
     const double2* __restrict__ dinv = reinterpret_cast<const double2*>(a.A.dinv64);
+    const double2 one = make_double2(1.0, 1.0);
     double* const part0 = a.part;
     double* const part1 = a.part + kMaxBlocks;
-    double* const part2 = a.part + 3 * kMaxBlocks;  // own slot: L1 may overwrite [0, G) early
+    // own slot: L1 may overwrite [0, G) early; the check runs between the L2
+    // barrier and L3, when no block can be writing part0 or part1's readers
+    // still need them
+    double* const part2 = a.part + 3 * kMaxBlocks;
 
     if (threadIdx.x == 0) {
-        sc.gq = sc.gg = sc.bb = sc.target2 = 0.0;
-        sc.k = 0;
+        sc.gq = sc.gq_old = sc.gg = sc.bb = sc.target2 = sc.report = 0.0;
+        sc.k = sc.checks = 0;
     }
     {   // init: g = A x - b, q = g / Aii, p = -q
         double v[3] = {0.0, 0.0, 0.0};  // gq, gg, bb
@@ -68,9 +93,9 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
             const uint32_t i = s * 32 + lane;
             if (i >= Nn) continue;
             const double2 ax = spmv_row_f64(a.A, s, lane, x);
-            const double2 bi = b[i], di = dinv[i];
+            const double2 bi = b[i];
             const double2 gi = make_double2(ax.x - bi.x, ax.y - bi.y);
-            const double2 qi = make_double2(gi.x * di.x, gi.y * di.y);
+            const double2 qi = precond<JAC>(gi, JAC ? dinv[i] : one);
             g[i] = gi;
             q[i] = qi;
             p[i] = make_double2(-qi.x, -qi.y);
@@ -89,7 +114,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
         group_reduce0<3>(part2, G, t);
         if (threadIdx.x == 0) {
             sc.gq = t[0];
-            sc.gg = t[1];
+            sc.gg = sc.report = t[1];
             sc.bb = t[2];
             sc.target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * sc.bb : a.tol * a.tol;
             s_stop = !(sc.gg > sc.target2) || a.max_iter == 0;
@@ -124,13 +149,13 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane;
                 if (i >= Nn) continue;
-                const double2 pi = p[i], wi = w[i], di = dinv[i];
+                const double2 pi = p[i], wi = w[i];
                 double2 xi = x[i], gi = g[i];
                 xi.x = fma(alpha, pi.x, xi.x);
                 xi.y = fma(alpha, pi.y, xi.y);
                 gi.x = fma(alpha, wi.x, gi.x);
                 gi.y = fma(alpha, wi.y, gi.y);
-                const double2 qi = make_double2(gi.x * di.x, gi.y * di.y);
+                const double2 qi = precond<JAC>(gi, JAC ? dinv[i] : one);
                 x[i] = xi;
                 g[i] = gi;
                 q[i] = qi;
@@ -149,10 +174,52 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
             double t2[2];
             group_reduce0<2>(part1, G, t2);
             if (threadIdx.x == 0) {
-                s_coef = t2[0] / sc.gq;  // beta
+                sc.gq_old = sc.gq;
                 sc.gq = t2[0];
-                sc.gg = t2[1];
+                s_coef = t2[0] / sc.gq_old;  // beta
                 sc.k++;
+                if (LAGGED) {
+                    const double lag = sc.gg;  // ||g_{k-1}||^2, as nbots tests it
+                    sc.gg = t2[1];
+                    sc.report = lag;
+                    s_stop = !(lag > sc.target2) || sc.k >= a.max_iter;
+                } else {
+                    sc.gg = sc.report = t2[1];
+                    s_stop = !(sc.gg > sc.target2) ? 2 : (sc.k >= a.max_iter ? 1 : 0);
+                }
+            }
+            __syncthreads();
+        }
+        if (!LAGGED && s_stop == 2) {
+            // confirm on the true residual: x is complete (written before the
+            // L2 barrier) and nobody writes it again before the next L2
+            double v[2] = {0.0, 0.0};
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane;
+                if (i >= Nn) continue;
+                const double2 ax = spmv_row_f64(a.A, s, lane, x);
+                const double2 bi = b[i];
+                const double2 gi = make_double2(ax.x - bi.x, ax.y - bi.y);
+                const double2 qi = precond<JAC>(gi, JAC ? dinv[i] : one);
+                g[i] = gi;
+                q[i] = qi;
+                v[0] = fma(gi.x, qi.x, fma(gi.y, qi.y, v[0]));
+                v[1] = fma(gi.x, gi.x, fma(gi.y, gi.y, v[1]));
+            }
+            double t[2];
+            block_sum_f64<2>(v, buf, t);
+            if (threadIdx.x == 0) {
+                part2[blockIdx.x * 2] = t[0];
+                part2[blockIdx.x * 2 + 1] = t[1];
+            }
+            if (grid_barrier(a.bar, G, blockIdx.x, a.status)) goto done;
+            double t2[2];
+            group_reduce0<2>(part2, G, t2);
+            if (threadIdx.x == 0) {
+                sc.checks++;
+                sc.gq = t2[0];
+                sc.gg = sc.report = t2[1];
+                s_coef = t2[0] / sc.gq_old;  // beta from the replaced residual
                 s_stop = !(sc.gg > sc.target2) || sc.k >= a.max_iter;
             }
             __syncthreads();
@@ -173,9 +240,10 @@ done:
     if (blockIdx.x == 0 && threadIdx.x == 0) {
         a.res[0] = (double)sc.k;
         int st = ld_volatile(a.status);
-        a.res[1] = st != 0 ? (double)st : (sc.gg > sc.target2 ? 1.0 : 0.0);
-        a.res[2] = sc.gg;
+        a.res[1] = st != 0 ? (double)st : (sc.report > sc.target2 ? 1.0 : 0.0);
+        a.res[2] = sc.report;
         a.res[3] = sc.bb;
+        a.res[4] = (double)sc.checks;
     }
 }
 
@@ -196,7 +264,7 @@ extern "C" int nbg_cg_bsr_f64(const nbg_bsr_t* A, const double* b, double* x, ui
     if (!result || !A) return NBG_ERR_ARG;
     *result = nbg_cg_result_t{0, 0, 0.0, 0.0};
     if (A->Nn == 0) return NBG_OK;
-    if (!A->b64 || !A->dinv64) return NBG_ERR_ARG;
+    if (!A->b64 || ((flags & NBG_CG_JACOBI) && !A->dinv64)) return NBG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t need = cg_bsr_bytes(A->N);
     void* own = nullptr;
@@ -226,7 +294,7 @@ extern "C" int nbg_cg_bsr_f64(const nbg_bsr_t* A, const double* b, double* x, ui
     a.flags = flags;
     int rc = NBG_OK;
     unsigned G = 1;
-    double hr[4] = {0, 0, 0, 0};
+    double hr[5] = {0, 0, 0, 0, 0};
     cudaError_t e = cudaMemsetAsync(tail, 0, 3 * 256, s);
     if (A->perm) {  // solve in the layout's node order
         double* bp = (double*)(base + cg_bsr_core_bytes(A->N));
@@ -236,11 +304,15 @@ extern "C" int nbg_cg_bsr_f64(const nbg_bsr_t* A, const double* b, double* x, ui
         a.b = bp;
         a.x = xp;
     }
-    if (e == cudaSuccess) rc = coop_grid((const void*)k_cg_bsr_f64, A->n_slices, &G);
+    const bool jac = (flags & NBG_CG_JACOBI) != 0, lagged = (flags & NBG_CG_NBOTS_STOP) != 0;
+    const void* fn = jac ? (lagged ? (const void*)k_cg_bsr_f64<true, true>
+                                   : (const void*)k_cg_bsr_f64<true, false>)
+                         : (lagged ? (const void*)k_cg_bsr_f64<false, true>
+                                   : (const void*)k_cg_bsr_f64<false, false>);
+    if (e == cudaSuccess) rc = coop_grid(fn, A->n_slices, &G);
     if (e == cudaSuccess && rc == NBG_OK) {
         void* args[] = {&a};
-        e = cudaLaunchCooperativeKernel((const void*)k_cg_bsr_f64, dim3(G), dim3(kPersistThreads),
-                                        args, 0, s);
+        e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kPersistThreads), args, 0, s);
         if (e == cudaSuccess && A->perm) e = perm_scatter(A->Nn, A->perm, (const double*)a.x, x, s);
     }
     if (e == cudaSuccess && rc == NBG_OK)

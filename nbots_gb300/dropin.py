@@ -242,32 +242,53 @@ class NbotsObjects:
 
 def nodal_graph(p: Problem):
     """nb_mesh2D_load_graph(NB_NODES_LINKED_BY_ELEMS) of a problem's mesh
-    (load_graph.c:230-328), as an nb_graph_t with its buffers."""
+    (load_graph.c:230-328), as an nb_graph_t with its buffers: both ends of
+    every edge, and for elements with more than three nodes the opposite
+    corners.  Built with array operations (each node's neighbours in edge
+    order, then element order); nb_sparse_create sorts the rows."""
     nen = p.conn.shape[1]
-    adj = [[] for _ in range(p.n_nodes)]
-    for a, b in p.edges:
-        adj[int(a)].append(int(b))
-        adj[int(b)].append(int(a))
+    e = np.asarray(p.edges, np.int64).reshape(-1, 2)
+    src = [e[:, 0], e[:, 1]]
+    dst = [e[:, 1], e[:, 0]]
     if nen > 3:
-        for e in p.conn:
-            for i in range(nen):
-                for j in range(nen - 3):
-                    adj[int(e[i])].append(int(e[(i + j + 2) % nen]))
-    n_adj = np.array([len(a) for a in adj], np.uint32)
-    rows = [np.array(a, np.uint32) for a in adj]
-    ptrs = (C.POINTER(u32) * p.n_nodes)(*[r.ctypes.data_as(C.POINTER(u32)) for r in rows])
-    g = Graph(p.n_nodes, n_adj.ctypes.data_as(C.POINTER(u32)), ptrs, None, None)
-    return g, (n_adj, rows, ptrs)
+        conn = np.asarray(p.conn, np.int64)
+        for i in range(nen):
+            for j in range(nen - 3):
+                src.append(conn[:, i])
+                dst.append(conn[:, (i + j + 2) % nen])
+    src = np.concatenate(src)
+    dst = np.concatenate(dst)
+    order = np.argsort(src, kind="stable")
+    n_adj = np.bincount(src, minlength=p.n_nodes).astype(np.uint32)
+    flat = np.ascontiguousarray(dst[order], np.uint32)
+    off = np.zeros(p.n_nodes, np.uint64)
+    off[1:] = np.cumsum(n_adj[:-1], dtype=np.uint64)
+    addr = np.ascontiguousarray(flat.ctypes.data + 4 * off, np.uint64)
+    g = Graph(p.n_nodes, n_adj.ctypes.data_as(C.POINTER(u32)),
+              C.cast(addr.ctypes.data, C.POINTER(C.POINTER(u32))), None, None)
+    return g, (n_adj, flat, addr)
 
 
 def sparse_from_csr(p: Problem, values):
     """nb_sparse_create on the problem's nodal graph, filled with CSR values
-    in row order."""
+    in row order (one copy into the slab when the rows sit in it in order,
+    as nb_sparse_create lays them out)."""
     G, _ = libs()
     g, keep = nodal_graph(p)
     A = G.nb_sparse_create(C.byref(g), None, 2)
+    N = A.contents.N
+    values = np.ascontiguousarray(values, np.float64)
+    sizes = np.ctypeslib.as_array(A.contents.rows_size, shape=(N,)).astype(np.uint64)
+    offs = np.zeros(N, np.uint64)
+    offs[1:] = np.cumsum(sizes[:-1])
+    rows = np.ctypeslib.as_array(C.cast(A.contents.rows_values, C.POINTER(C.c_uint64)),
+                                 shape=(N,))
+    base = C.cast(A.contents.rows_values[0], C.c_void_p).value
+    if np.array_equal(rows, base + 8 * offs):
+        C.memmove(base, values.ctypes.data, values.nbytes)
+        return A, keep
     o = 0
-    for i in range(A.contents.N):
+    for i in range(N):
         n = A.contents.rows_size[i]
         row = np.ctypeslib.as_array(A.contents.rows_values[i], shape=(n,))
         row[:] = values[o:o + n]

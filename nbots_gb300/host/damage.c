@@ -116,8 +116,10 @@ int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, doub
 		   double rtol, int method, const char *logfile, nbg_damage_info_t *info)
 {
 	int rc = NBG_OK;
-	if (!f || !bcs || (method != NBG_METHOD_NBOTS && method != NBG_METHOD_FP64))
+	if (!f || !bcs || (method != NBG_METHOD_NBOTS && method != NBG_METHOD_FP64 &&
+			   method != NBG_METHOD_NBOTS_FAST))
 		return NBG_ERR_ARG;
+	const int blocked = method != NBG_METHOD_NBOTS;
 	nbg_damage_info_t inf;
 	memset(&inf, 0, sizeof(inf));
 	dmg_ws_t w;
@@ -142,7 +144,7 @@ int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, doub
 	w.norm2 = w.rws + nbg_residual_workspace_bytes(N) / 8;
 	TRY(nbg_fem_cg_workspace(f));
 	const size_t bws_bytes = nbg_cg_bsr_workspace_bytes(N);
-	if (method == NBG_METHOD_FP64)
+	if (blocked)
 		TRY(nbg_dev_alloc((void **)&w.bws, bws_bytes));
 	Eh = malloc(8 * (size_t)(ne ? ne : 1));
 	rh = malloc(8 * (npt ? npt : 1));
@@ -194,10 +196,13 @@ int nbg_fem_damage(nbg_fem_t *f, const nbg_bcs_t *bcs, double E, double nu, doub
 			/* returns 1 (and cg.status 1) when the tolerance is not reached */
 			nbg_cg_result_t cg;
 			int st;
-			if (method == NBG_METHOD_FP64) {
+			if (blocked) {
 				TRY(nbg_fem_block_layout(f, NULL));  /* from this K */
-				st = nbg_cg_bsr_f64(&f->bsr, w.res, w.du, N, 1e-8, NBG_CG_JACOBI, &cg,
-						    w.bws, bws_bytes, f->stream);
+				st = nbg_cg_bsr_f64(&f->bsr, w.res, w.du, N, 1e-8,
+						    method == NBG_METHOD_NBOTS_FAST
+							    ? NBG_CG_JACOBI | NBG_CG_NBOTS_STOP
+							    : NBG_CG_JACOBI,
+						    &cg, w.bws, bws_bytes, f->stream);
 			} else {
 				st = nbg_cg_f64(N, f->row_ptr, f->col_idx, f->K, w.res, w.du, N, 1e-8,
 						NBG_CG_JACOBI, &cg, f->cg_ws, f->cg_ws_bytes, f->stream);

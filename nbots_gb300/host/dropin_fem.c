@@ -19,6 +19,13 @@ void nbg_dropin_record_error(int e);
 int nbg_dropin_cpu(void);
 void *nbg_dropin_next(const char *name);
 
+/* NBG_DROPIN_EXACT_CG=1: nbots' arithmetic on the CSR for every drop-in CG */
+static int exact_cg(void)
+{
+	const char *v = getenv("NBG_DROPIN_EXACT_CG");
+	return v && v[0] == '1' && v[1] == 0;
+}
+
 typedef struct {
 	nbg_mesh_t m;
 	double *nod;
@@ -221,9 +228,13 @@ int nb_fem_compute_2D_Solid_Mechanics(const nb_mesh2D_t *part, const nb_fem_elem
 	}
 	if (rc == NBG_OK) {
 		/* solver() of static_elasticity2D.c:83-97: x0 = 0, max_iter = N,
-		 * tol 1e-8 absolute; "not converged" counts as success */
+		 * tol 1e-8 absolute; "not converged" counts as success.  nbots'
+		 * iteration and stop test, on the block layout with FMAs unless
+		 * NBG_DROPIN_EXACT_CG=1 asks for nbots' arithmetic on the CSR */
 		nbg_cg_result_t r;
-		int st = nbg_fem_solve(f, nbg_fem_n_dof(f), 1e-8, NBG_CG_JACOBI, &r);
+		int st = exact_cg() ? nbg_fem_solve(f, nbg_fem_n_dof(f), 1e-8, NBG_CG_JACOBI, &r)
+				    : nbg_fem_solve_fast(f, nbg_fem_n_dof(f), 1e-8,
+							 NBG_CG_JACOBI | NBG_CG_NBOTS_STOP, &r);
 		rc = st < 0 ? st : NBG_OK;
 	}
 	if (rc == NBG_OK)
@@ -367,8 +378,9 @@ void nb_fem_compute_2D_Non_Linear_Solid_Mechanics(const nb_mesh2D_t *part,
 				    nb_fem_implicit_get_N_steps(params),
 				    nb_fem_implicit_get_N_max_iter(params),
 				    nb_fem_implicit_get_N_max_iter_without_enhance(params),
-				    nb_fem_implicit_get_residual_tolerance(params), NBG_METHOD_NBOTS,
-				    logfile, &info);
+				    nb_fem_implicit_get_residual_tolerance(params),
+				    exact_cg() ? NBG_METHOD_NBOTS : NBG_METHOD_NBOTS_FAST, logfile,
+				    &info);
 	}
 	nbg_dropin_record_error(rc);
 	nbg_fem_destroy(f);

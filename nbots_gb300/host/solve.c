@@ -1,9 +1,11 @@
 /*
  * Host-buffer solver context: a CSR system in host memory (the layout of
  * nb_sparse_create(graph, NULL, 2), sparse.c:20-60) is uploaded, converted
- * to the device block layout and solved by one of the three CG kernels; x
- * comes back to host memory.  The device buffers are kept between calls, and
- * so is the pattern when the caller says it has not changed.
+ * to the device block layout and solved by one of the CG kernels (nbots'
+ * arithmetic on the CSR, nbots' iteration or the fast FP64 CG on the block
+ * layout, mixed precision); x comes back to host memory.  The device buffers
+ * are kept between calls, and so is the pattern when the caller says it has
+ * not changed.  The drop-in nb_sparse_* entries keep one context per matrix.
  */
 #include <stdlib.h>
 #include <string.h>
@@ -110,6 +112,8 @@ int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
 		free(so);
 		s->have_pattern = 1;
 	}
+	if (!val)  /* values to come from the device side (nbg_solver_device_csr) */
+		return nbg_stream_sync(s->stream);
 	TRY(nbg_h2d(s->val, val, 8 * nnz, s->stream));
 	if (s->bsr_ok)
 		TRY(nbg_bsr_fill(&s->bsr, s->rp, s->ci, s->val, s->stream));
@@ -126,11 +130,15 @@ int nbg_solver_solve(nbg_solver_t *s, const double *b, double *x, uint32_t max_i
 	memset(info, 0, sizeof(*info));
 	if (!s->have_pattern)
 		return NBG_ERR_ARG;
+	/* nbots' iteration runs on the block layout when the pattern has one,
+	 * else on the CSR with nbots' own arithmetic */
+	if (method == NBG_METHOD_NBOTS_FAST && !s->bsr_ok)
+		method = NBG_METHOD_NBOTS;
 	if (method != NBG_METHOD_NBOTS && !s->bsr_ok)
 		return NBG_ERR_PATTERN;
 	size_t need = method == NBG_METHOD_NBOTS ? nbg_cg_workspace_bytes(s->N)
-		    : method == NBG_METHOD_FP64 ? nbg_cg_bsr_workspace_bytes(s->N)
-		    : nbg_cg_mixed_workspace_bytes(s->N);
+		    : method == NBG_METHOD_MIXED ? nbg_cg_mixed_workspace_bytes(s->N)
+		    : nbg_cg_bsr_workspace_bytes(s->N);
 	if (s->ws_bytes < need) {
 		nbg_dev_free(s->ws);
 		s->ws = NULL;
@@ -155,8 +163,10 @@ int nbg_solver_solve(nbg_solver_t *s, const double *b, double *x, uint32_t max_i
 			rc = nbg_cg_f64(s->N, s->rp, s->ci, s->val, s->b, s->x, max_iter, tol, flags,
 					&r, s->ws, s->ws_bytes, s->stream);
 		else
-			rc = nbg_cg_bsr_f64(&s->bsr, s->b, s->x, max_iter, tol, flags, &r, s->ws,
-					    s->ws_bytes, s->stream);
+			rc = nbg_cg_bsr_f64(&s->bsr, s->b, s->x, max_iter, tol,
+					    method == NBG_METHOD_NBOTS_FAST ? flags | NBG_CG_NBOTS_STOP
+									   : flags,
+					    &r, s->ws, s->ws_bytes, s->stream);
 		info->niter = r.niter;
 		info->status = r.status;
 		info->tol_reached = r.tol_reached;
@@ -170,4 +180,52 @@ int nbg_solver_solve(nbg_solver_t *s, const double *b, double *x, uint32_t max_i
 	return r2 != NBG_OK ? r2 : rc;
 fail:
 	return rc;
+}
+
+int nbg_solver_multiply(nbg_solver_t *s, const double *in, double *out)
+{
+	if (!s->have_pattern)
+		return NBG_ERR_ARG;
+	if (s->N == 0)
+		return NBG_OK;
+	int rc = nbg_h2d(s->x, in, 8 * (size_t)s->N, s->stream);
+	if (rc == NBG_OK)
+		rc = nbg_spmv_csr_f64(s->N, s->rp, s->ci, s->val, s->x, s->b, s->stream);
+	if (rc == NBG_OK)
+		rc = nbg_d2h(out, s->b, 8 * (size_t)s->N, s->stream);
+	if (rc == NBG_OK)
+		rc = nbg_stream_sync(s->stream);
+	return rc;
+}
+
+int nbg_solver_device_csr(nbg_solver_t *s, const uint32_t **row_ptr, const uint32_t **col_idx,
+			  double **val)
+{
+	if (!s->have_pattern)
+		return NBG_ERR_ARG;
+	if (row_ptr)
+		*row_ptr = s->rp;
+	if (col_idx)
+		*col_idx = s->ci;
+	if (val)
+		*val = s->val;
+	return NBG_OK;
+}
+
+int nbg_solver_values_changed(nbg_solver_t *s)
+{
+	if (!s->have_pattern)
+		return NBG_ERR_ARG;
+	return s->bsr_ok ? nbg_bsr_fill(&s->bsr, s->rp, s->ci, s->val, s->stream) : NBG_OK;
+}
+
+size_t nbg_solver_device_bytes(const nbg_solver_t *s)
+{
+	if (!s->have_pattern)
+		return s->ws_bytes;
+	size_t b = 4 * ((size_t)s->N + 1) + 12 * (size_t)s->nnz + 16 * (size_t)s->N + s->ws_bytes;
+	if (s->bsr_ok)
+		b += 4 * ((size_t)s->bsr.n_slices + 1) + 60 * (size_t)s->bsr.n_entries +
+		     12 * (size_t)s->N;
+	return b;
 }

@@ -1,6 +1,7 @@
 """Regenerates tests/golden/*.npz from the reference nbots library.
 
-Run in a container that holds the nbots sources (default /root/reference):
+Run where the nbots sources are (NBOTS_SRC in the environment, --nbots-src,
+or oracle/Makefile.ref's default location):
 
     python tests/golden/make_golden.py [--nbots-src DIR]
 
@@ -126,12 +127,13 @@ def save(name, prob_path, dump):
 
 def main():
     ap = argparse.ArgumentParser()
-    ap.add_argument("--nbots-src", default="/root/reference")
+    ap.add_argument("--nbots-src", default=os.environ.get("NBOTS_SRC"),
+                    help="nbots source tree (default: $NBOTS_SRC, else the build recipe's)")
     ap.add_argument("--only", nargs="*", help="regenerate these cases only")
     a = ap.parse_args()
     want = (lambda name: True) if not a.only else (lambda name: name in a.only)
-    run(["make", "-s", "-C", ROOT, "-f", "oracle/Makefile.ref", f"NBOTS_SRC={a.nbots_src}",
-         "-j8", "harness"])
+    run(["make", "-s", "-C", ROOT, "-f", "oracle/Makefile.ref"] +
+        ([f"NBOTS_SRC={a.nbots_src}"] if a.nbots_src else []) + ["-j8", "harness"])
     tmp = tempfile.mkdtemp()
     for name, p in small_cases().items():
         if not want(name):

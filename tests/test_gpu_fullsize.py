@@ -1,9 +1,15 @@
 """Parity at the benchmark's full size: the 1024x512 Q4 cantilever
 (1,051,650 dof, lognormal E).  The device pattern equals the host build
 word for word; K and F after assembly and boundary conditions and the
-nbots-order SpMV equal the oracle's bit for bit; the mixed solve reaches
-relres 1e-8 on the true FP64 residual and lands within 1e-8 (relative L2)
-of the fast FP64 solution at the same tolerance."""
+nbots-order SpMV equal the oracle's bit for bit; nbots' Jacobi-PCG on the
+GPU (operation for operation on the CSR, and nbots' iteration on the block
+layout, the drop-in's solver) lands within 1e-10 (relative L2) of the
+oracle's run of the same loop, with an iteration count within 10 %; the
+fast FP64 CG stops on a true residual below its target; the mixed solve
+reaches relres 1e-8 on the true FP64 residual and lands within 1e-8 of the
+fast FP64 solution at the same tolerance."""
+import os
+
 import numpy as np
 import pytest
 
@@ -65,3 +71,43 @@ def test_full_size_mixed_solve(c2):
                                      s.dptr(L.FEM_K), du.ptr, dy.ptr, None), "spmv")
     assert np.linalg.norm(F - dy.numpy()) <= 1.05e-8 * np.linalg.norm(F)
     assert np.linalg.norm(um - u64) <= 1e-8 * np.linalg.norm(u64)
+
+
+def test_full_size_nbots_cg_against_oracle(c2):
+    """nbots' loop at 1M dof: absolute tolerance 1e-8 ||F|| (relres 1e-8),
+    x0 = 0, max_iter = N; the oracle (pinned bit for bit to nbots' own runs
+    on the fixtures) runs it on all host threads."""
+    from nbots_gb300 import _lib as L
+    from nbots_gb300.device import DeviceArray
+    p, s = c2
+    if s.assemble() != 0:
+        pytest.fail("assembly")
+    s.apply_bcs()
+    fl = O.Flat(p)
+    rp, ci = O.pattern(fl)
+    _, K, F = O.assemble(fl, rp, ci)
+    O.set_bconditions(fl, rp, ci, K, F)
+    tol = 1e-8 * np.linalg.norm(F)
+    u_ref, it_ref, _, st_ref = O.cg_jacobi(rp, ci, K, F, tol=tol, threads=os.cpu_count())
+    assert st_ref == 0
+    # k_cg_f64: nbots' arithmetic on the CSR
+    r = s.solve(tol=tol)
+    u = s.get(L.FEM_U)
+    assert r.status == 0
+    assert abs(int(r.niter) - it_ref) <= it_ref // 10, (r.niter, it_ref)
+    assert np.linalg.norm(u - u_ref) <= 1e-10 * np.linalg.norm(u_ref)
+    # k_cg_bsr_f64 with nbots' stop rule: the drop-in's solver
+    r = s.solve_fast(tol=tol, flags=L.CG_JACOBI | L.CG_NBOTS_STOP)
+    u = s.get(L.FEM_U)
+    assert r.status == 0
+    assert abs(int(r.niter) - it_ref) <= it_ref // 10, (r.niter, it_ref)
+    assert np.linalg.norm(u - u_ref) <= 1e-10 * np.linalg.norm(u_ref)
+    # the fast stop rule: the reported norm is the true residual's
+    r = s.solve_fast(tol=1e-8)
+    u = s.get(L.FEM_U)
+    du, dy = DeviceArray(u), DeviceArray(shape=(s.N,), dtype=np.float64)
+    L.check(L.lib().nbg_spmv_csr_f64(s.N, s.dptr(L.FEM_ROW_PTR), s.dptr(L.FEM_COL_IDX),
+                                     s.dptr(L.FEM_K), du.ptr, dy.ptr, None), "spmv")
+    true_res = np.linalg.norm(F - dy.numpy())
+    assert r.status == 0 and true_res <= 1e-8 * np.linalg.norm(F)
+    assert abs(r.tol_reached - true_res) <= 1e-3 * true_res

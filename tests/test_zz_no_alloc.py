@@ -7,7 +7,9 @@ static device array instead.  Here it is called twice in a row through the
 C ABI, on two different systems, and each result is compared with the
 allocating entry point's on the same inputs (u within 1e-10 relative L2,
 the tolerance of the other CG parity tests; the same iteration count and
-status).  A system larger than the array is refused with an error.
+status).  The device's free memory (cudaMemGetInfo) is the same before and
+after each call once the library's kernels are loaded: the calls allocate
+nothing.  A system larger than the array is refused with an error.
 
 The file sorts last so that a run stopping at the first failure has run
 every other test before it; it also passes alone in a fresh process.
@@ -26,11 +28,18 @@ def rel(a, b):
     return float(np.linalg.norm(a - b) / np.linalg.norm(b))
 
 
+def free_device_bytes():
+    import torch
+    torch.cuda.synchronize()
+    return torch.cuda.mem_get_info()[0]
+
+
 def test_noalloc_cg_matches_allocating_entry_on_two_calls():
     from nbots_gb300 import _lib as L
     from nbots_gb300.device import DeviceArray
     lib = L.lib()
     assert lib.nbg_device_count() > 0
+    free_device_bytes()  # the harness's own CUDA state, before any measurement
     for name in ("c1_q4_64x32", "q4_allbc_16x8"):
         _, d = load_golden(name)
         N = d["F_bc"].shape[0]
@@ -41,8 +50,10 @@ def test_noalloc_cg_matches_allocating_entry_on_two_calls():
         r_ref, r_na = L.CgResult(), L.CgResult()
         rc_ref = lib.nbg_cg_f64(N, rp.ptr, ci.ptr, K.ptr, F.ptr, x_ref.ptr, N, 1e-8,
                                 L.CG_JACOBI, C.byref(r_ref), None, 0, None)
+        free0 = free_device_bytes()
         rc_na = lib.nbg_cg_f64_noalloc(N, rp.ptr, ci.ptr, K.ptr, F.ptr, x_na.ptr, N, 1e-8,
                                        L.CG_JACOBI, C.byref(r_na), None)
+        assert free_device_bytes() == free0
         assert rc_ref == rc_na == 0
         assert (r_na.niter, r_na.status) == (r_ref.niter, r_ref.status)
         u_ref, u_na = x_ref.numpy(), x_na.numpy()
