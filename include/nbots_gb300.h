@@ -267,7 +267,9 @@ int nbg_spmv_bsr_f32(const nbg_bsr_t *A, const float *x, float *y, void *stream)
  * stop: the current ||g|| meets the target and the true residual b - A x,
  * recomputed in FP64 at that point, meets it too (else that residual
  * replaces the recurrence's and the iteration goes on); tol_reached is then
- * the true residual norm.  With NBG_CG_NBOTS_STOP: nbots' iteration and stop
+ * the true residual norm.  A target below the FP64 floor of the system (the
+ * true residual stops falling between two such checks) ends the solve with
+ * status 1 and that floor in tol_reached.  With NBG_CG_NBOTS_STOP: nbots' iteration and stop
  * test (the lagged ||g||, one iteration past the first ||g|| <= tol),
  * iterates within rounding of nbots' own.  NBG_CG_RELATIVE selects
  * ||g|| <= tol ||b||.  x holds x0 on entry. */
@@ -379,6 +381,10 @@ int nbg_solver_multiply(nbg_solver_t *s, const double *in, double *out);
 int nbg_solver_device_csr(nbg_solver_t *s, const uint32_t **row_ptr, const uint32_t **col_idx,
                           double **val);
 int nbg_solver_values_changed(nbg_solver_t *s);
+/* The solver's block layout (current with its values), or NBG_ERR_PATTERN
+ * when the pattern is not node-blocked (two rows per node with the same
+ * column pairs) or NBG_CSR_ONLY was set. */
+int nbg_solver_block_layout(nbg_solver_t *s, nbg_bsr_t *out);
 /* Device bytes the solver holds (matrix, block layout, vectors, workspace). */
 size_t nbg_solver_device_bytes(const nbg_solver_t *s);
 
@@ -537,7 +543,9 @@ typedef struct {
 /* Objective and its gradient for densities rho (host arrays): assemble with
  * E(rho), apply the boundary conditions (homogeneous Dirichlet values),
  * solve K u = F (and K lambda = e_dof) with `method` (NBG_METHOD_FP64 or
- * NBG_METHOD_MIXED) to relative tolerance tol, write dJ/drho to dJ. */
+ * NBG_METHOD_MIXED) to relative tolerance tol, write dJ/drho to dJ.  Returns
+ * 0, 1 when a solve stopped short of tol (at the solver's iteration limit
+ * or FP64 floor; J and dJ are still computed from it), or an error. */
 int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double nu,
                  double thickness, double penal, double E0, double Emin, int objective,
                  uint32_t dof, double tol, int method, double *dJ, nbg_simp_info_t *info);

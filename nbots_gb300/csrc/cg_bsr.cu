@@ -23,7 +23,10 @@
 //    pass recomputes g = A x - b (and q, g.q, g.g) from x; if the true norm
 //    is still above the target, g replaces the recurrence's residual and the
 //    iteration continues with beta from the true g.q (residual replacement),
-//    so the reported norm is always a true FP64 residual.
+//    so the reported norm is always a true FP64 residual.  A target below
+//    what FP64 can reach on the system shows as a second failed check with
+//    a true residual not even halved since the first: the solve then stops,
+//    not converged (status 1), reporting that floor.
 // JAC = false is the unpreconditioned CG (q = g).
 #include <cstdint>
 
@@ -59,7 +62,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
     __shared__ double s_coef;  // alpha, then beta
     __shared__ int s_stop;     // 0 iterate, 1 stop, 2 confirm on the true residual first
     __shared__ struct {
-        double gq, gq_old, gg, bb, target2, report;
+        double gq, gq_old, gg, bb, target2, report, gg_check;
         uint32_t k, checks;
     } sc;  // scalar state, thread 0 only
     const unsigned G = gridDim.x;
@@ -84,7 +87,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
     double* const part2 = a.part + 3 * kMaxBlocks;
 
     if (threadIdx.x == 0) {
-        sc.gq = sc.gq_old = sc.gg = sc.bb = sc.target2 = sc.report = 0.0;
+        sc.gq = sc.gq_old = sc.gg = sc.bb = sc.target2 = sc.report = sc.gg_check = 0.0;
         sc.k = sc.checks = 0;
     }
     {   // init: g = A x - b, q = g / Aii, p = -q
@@ -220,7 +223,13 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
                 sc.gq = t2[0];
                 sc.gg = sc.report = t2[1];
                 s_coef = t2[0] / sc.gq_old;  // beta from the replaced residual
-                s_stop = !(sc.gg > sc.target2) || sc.k >= a.max_iter;
+                // the recurrence fell below the target again but the true
+                // residual did not follow (not even halved since the last
+                // check): it sits at its FP64 floor above the target
+                const bool stalled = sc.checks > 1 && !(sc.gg < 0.25 * sc.gg_check);
+                sc.gg_check = sc.gg;
+                s_stop = !(sc.gg > sc.target2) || stalled || sc.k >= a.max_iter ||
+                         sc.checks >= 64;
             }
             __syncthreads();
         }

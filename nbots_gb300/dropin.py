@@ -81,6 +81,17 @@ def libs():
             vp, vp, vp, vp, b8, vp, b8, C.c_int, C.POINTER(Params2D), vp, C.c_char_p]
         G.nb_fem_compute_2D_Non_Linear_Solid_Mechanics.restype = None
         G.nbg_dropin_error.restype = C.c_int
+        G.pipeline_assemble_system.argtypes = [sp, vp, vp, vp, vp, vp, b8, vp, C.c_int,
+                                               C.POINTER(Params2D), vp]
+        G.pipeline_assemble_system.restype = C.c_int
+        G.nb_fem_set_bconditions.argtypes = [vp, sp, vp, vp, f64]
+        G.nb_fem_set_bconditions.restype = None
+        G.pipeline_compute_strain.argtypes = [vp, vp, vp, vp]
+        G.pipeline_compute_strain.restype = None
+        G.nb_sparse_scale.argtypes = [sp, f64]
+        G.nb_sparse_scale.restype = None
+        G.nbg_dropin_sparse_touch.argtypes = [sp]
+        G.nbg_dropin_sparse_touch.restype = None
         H.nbh_mesh2D_create.argtypes = [u32, u32, vp, u32, vp, u32, vp, u32, vp, u32, vp, vp]
         H.nbh_mesh2D_create.restype = vp
         H.nb_mesh2D_destroy.argtypes = [vp]
@@ -187,6 +198,33 @@ class NbotsObjects:
                                                  None if en is None else en.ctypes.data,
                                                  u.ctypes.data, strain.ctypes.data)
         return st, u, strain
+
+    def pipeline(self, K, F):
+        """pipeline_assemble_system on the nbots matrix K and host vector F
+        (as nb_fem_compute_2D_Solid_Mechanics calls it): the status."""
+        G, _ = libs()
+        p = self.p
+        grav = (f64 * 2)(*p.gravity)
+        params = Params2D(p.thickness, 0.0, b"\0")
+        en = None if p.enabled is None else np.ascontiguousarray(p.enabled, np.bool_)
+        self._en = en
+        return G.pipeline_assemble_system(K, None, F.ctypes.data, self.mesh, self.elem,
+                                          self.mat, bool(p.self_weight), C.addressof(grav), 0,
+                                          C.byref(params),
+                                          None if en is None else en.ctypes.data)
+
+    def set_bconditions(self, K, F, factor=1.0):
+        G, _ = libs()
+        G.nb_fem_set_bconditions(self.mesh, K, F.ctypes.data, self.bcond, factor)
+
+    def strain_of(self, u):
+        G, _ = libs()
+        p = self.p
+        ngp = 4 if p.conn.shape[1] == 4 else 1
+        out = np.zeros(3 * ngp * p.n_elems)
+        u = np.ascontiguousarray(u, np.float64)
+        G.pipeline_compute_strain(out.ctypes.data, self.mesh, u.ctypes.data, self.elem)
+        return out
 
     def damage(self, ft, gf, n_steps, max_iter, max_iter_noenh, rtol, logfile):
         """nb_fem_compute_2D_Non_Linear_Solid_Mechanics through the drop-in

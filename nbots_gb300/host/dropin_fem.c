@@ -15,9 +15,16 @@
 #include "nbots_dropin.h"
 #include "nbots_gb300.h"
 
+#include "fem_internal.h"
+
 void nbg_dropin_record_error(int e);
 int nbg_dropin_cpu(void);
 void *nbg_dropin_next(const char *name);
+
+/* The device copy of a drop-in matrix (dropin_sparse.c). */
+nbg_solver_t *nbg_dropin_lock_device(const nb_sparse_t *A, int send_values, int *rc);
+void nbg_dropin_unlock_device(const nb_sparse_t *A, int synced);
+int nbg_dropin_slab(const nb_sparse_t *A, double **vals, const uint32_t **row_ptr);
 
 /* NBG_DROPIN_EXACT_CG=1: nbots' arithmetic on the CSR for every drop-in CG */
 static int exact_cg(void)
@@ -385,4 +392,202 @@ void nb_fem_compute_2D_Non_Linear_Solid_Mechanics(const nb_mesh2D_t *part,
 	nbg_dropin_record_error(rc);
 	nbg_fem_destroy(f);
 	free_problem(&h);
+}
+
+
+/* ------------------------------------------- replaced: the pipeline stages */
+typedef int (*assemble_fn)(nb_sparse_t *, double *, double *, const nb_mesh2D_t *,
+			   const nb_fem_elem_t *, const nb_material_t *, bool, double[2],
+			   nb_analysis2D_t, nb_analysis2D_params *, const bool *);
+typedef void (*bcond_fn)(const nb_mesh2D_t *, nb_sparse_t *, double *, const nb_bcond_t *,
+			 double);
+typedef void (*strain_fn)(double *, const nb_mesh2D_t *, double *, const nb_fem_elem_t *);
+
+/* The device copy of K (a matrix of nb_sparse_create(graph, NULL, 2) on
+ * this mesh: node-blocked, 2 N_nod rows) and a FEM system on it; NULL when K
+ * is not such a matrix (the caller then goes to nbots' own stage). */
+static nbg_fem_t *fem_on_matrix(nb_sparse_t *K, const nbg_mesh_t *m, int send_values,
+				int need_incidence, nbg_solver_t **dev, int *rc)
+{
+	*rc = NBG_OK;
+	*dev = NULL;
+	if (K->N != 2 * m->N_nod)
+		return NULL;
+	nbg_solver_t *d = nbg_dropin_lock_device(K, send_values, rc);
+	if (!d)
+		return NULL;
+	const uint32_t *rp, *ci;
+	double *val;
+	nbg_fem_t *f = NULL;
+	if (nbg_solver_block_layout(d, NULL) != NBG_OK ||
+	    nbg_solver_device_csr(d, &rp, &ci, &val) != NBG_OK) {
+		nbg_dropin_unlock_device(K, 0);
+		return NULL;
+	}
+	double *vals;
+	const uint32_t *hrp;
+	nbg_dropin_slab(K, &vals, &hrp);
+	*rc = nbg_fem_create_on_csr(&f, m, hrp[K->N], (uint32_t *)rp, (uint32_t *)ci, val,
+				    need_incidence, NULL);
+	if (*rc != NBG_OK) {
+		nbg_dropin_unlock_device(K, 0);
+		return NULL;
+	}
+	*dev = d;
+	return f;
+}
+
+/* Device K and F back to the caller's matrix and vector; the device copy's
+ * block layout follows the new values. */
+static int write_back(nb_sparse_t *K, nbg_solver_t *dev, nbg_fem_t *f, double *F)
+{
+	double *vals;
+	const uint32_t *hrp;
+	nbg_dropin_slab(K, &vals, &hrp);
+	int rc = nbg_d2h(vals, f->K, 8 * (size_t)hrp[K->N], NULL);
+	if (rc == NBG_OK)
+		rc = nbg_d2h(F, f->F, 8 * (size_t)f->N, NULL);
+	if (rc == NBG_OK)
+		rc = nbg_solver_values_changed(dev);
+	if (rc == NBG_OK)
+		rc = nbg_stream_sync(NULL);
+	return rc;
+}
+
+int pipeline_assemble_system(nb_sparse_t *K, double *M, double *F, const nb_mesh2D_t *part,
+			     const nb_fem_elem_t *elemtype, const nb_material_t *material,
+			     bool enable_self_weight, double gravity[2],
+			     nb_analysis2D_t analysis2D, nb_analysis2D_params *params2D,
+			     const bool *elements_enabled)
+{
+	const uint32_t nen = nb_fem_elem_get_N_nodes(elemtype);
+	host_problem_t h;
+	memset(&h, 0, sizeof(h));
+	nbg_fem_t *f = NULL;
+	nbg_solver_t *dev = NULL;
+	int rc = NBG_OK;
+	/* the lumped mass (M) is not computed on the device: nbots' own stage
+	 * does it, as everything under the A/B switch */
+	if (!nbg_dropin_cpu() && M == NULL && (nen == 3 || nen == 4)) {
+		rc = read_mesh(part, nen, &h);
+		if (rc == NBG_OK)
+			f = fem_on_matrix(K, &h.m, 0, 1, &dev, &rc);
+	}
+	if (!f) {
+		free_problem(&h);
+		if (rc != NBG_OK)
+			return rc;
+		assemble_fn next = (assemble_fn)nbg_dropin_next("pipeline_assemble_system");
+		return next ? next(K, M, F, part, elemtype, material, enable_self_weight, gravity,
+				   analysis2D, params2D, elements_enabled)
+			    : NBG_ERR_ARG;
+	}
+	const uint32_t Ne = h.m.N_elem;
+	double *E = malloc(8 * (size_t)(Ne ? Ne : 1));
+	uint8_t *en = elements_enabled ? malloc(Ne ? Ne : 1) : NULL;
+	if (!E || (elements_enabled && !en))
+		rc = NBG_ERR_NOMEM;
+	for (uint32_t e = 0; rc == NBG_OK && e < Ne; e++) {
+		E[e] = nb_material_get_elasticity_module(material);
+		if (en)
+			en[e] = elements_enabled[e] ? 1 : 0;
+	}
+	int synced = 0;
+	if (rc == NBG_OK) {
+		double g2[2] = {gravity ? gravity[0] : 0.0, gravity ? gravity[1] : 0.0};
+		rc = nbg_fem_assemble(f, E, nb_material_get_poisson_module(material),
+				      params2D->thickness, nb_material_get_density(material),
+				      enable_self_weight, g2, en);
+		if (rc == NBG_OK) {
+			rc = write_back(K, dev, f, F);
+			synced = rc == NBG_OK;
+		} else if (rc == NBG_DISTORTED) {
+			/* nbots stops at the distorted element with K and F partly
+			 * summed; here they are left reset, and the status is its */
+			nb_sparse_reset(K);
+			memset(F, 0, 8 * (size_t)K->N);
+		}
+	}
+	nbg_fem_destroy(f);
+	nbg_dropin_unlock_device(K, synced);
+	free(E);
+	free(en);
+	free_problem(&h);
+	return rc;
+}
+
+void nb_fem_set_bconditions(const nb_mesh2D_t *part, nb_sparse_t *K, double *F,
+			    const nb_bcond_t *bcond, double factor)
+{
+	host_problem_t h;
+	memset(&h, 0, sizeof(h));
+	nbg_fem_t *f = NULL;
+	nbg_solver_t *dev = NULL;
+	int rc = NBG_OK;
+	const uint32_t nen = nb_mesh2D_get_N_elems(part) ? nb_mesh2D_elem_get_N_adj(part, 0) : 0;
+	if (!nbg_dropin_cpu() && (nen == 3 || nen == 4)) {
+		rc = read_mesh(part, nen, &h);
+		if (rc == NBG_OK)
+			rc = read_bcond(part, bcond, &h);
+		if (rc == NBG_OK)
+			f = fem_on_matrix(K, &h.m, 1, 0, &dev, &rc);
+	}
+	if (!f) {
+		free_problem(&h);
+		if (rc != NBG_OK) {
+			nbg_dropin_record_error(rc);
+			return;
+		}
+		bcond_fn next = (bcond_fn)nbg_dropin_next("nb_fem_set_bconditions");
+		if (next)
+			next(part, K, F, bcond, factor);
+		else
+			nbg_dropin_record_error(NBG_ERR_ARG);
+		return;
+	}
+	rc = nbg_h2d(f->F, F, 8 * (size_t)f->N, NULL);
+	nbg_bcs_t b = {h.vtx, h.N_sgm, h.sgm_ptr, h.sgm_nodes, h.N_bc, h.bc};
+	if (rc == NBG_OK)
+		rc = nbg_fem_apply_bcs(f, &b, factor);
+	if (rc == NBG_OK)
+		rc = write_back(K, dev, f, F);
+	nbg_fem_destroy(f);
+	nbg_dropin_unlock_device(K, rc == NBG_OK);
+	nbg_dropin_record_error(rc);
+	free_problem(&h);
+}
+
+void pipeline_compute_strain(double *strain, const nb_mesh2D_t *part, double *displacement,
+			     const nb_fem_elem_t *elemtype)
+{
+	const uint32_t nen = nb_fem_elem_get_N_nodes(elemtype);
+	if (nbg_dropin_cpu() || (nen != 3 && nen != 4)) {
+		strain_fn next = (strain_fn)nbg_dropin_next("pipeline_compute_strain");
+		if (next)
+			next(strain, part, displacement, elemtype);
+		else
+			nbg_dropin_record_error(NBG_ERR_ARG);
+		return;
+	}
+	host_problem_t h;
+	memset(&h, 0, sizeof(h));
+	int rc = read_mesh(part, nen, &h);
+	const size_t Nn = h.m.N_nod, Ne = h.m.N_elem, n3 = 3 * (size_t)(nen == 4 ? 4 : 1) * Ne;
+	void *dn = NULL, *dc = NULL, *du = NULL, *ds = NULL;
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&dn, 16 * (Nn ? Nn : 1));
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&dc, 4 * nen * (Ne ? Ne : 1));
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&du, 16 * (Nn ? Nn : 1));
+	if (rc == NBG_OK) rc = nbg_dev_alloc(&ds, 8 * (n3 ? n3 : 1));
+	if (rc == NBG_OK) rc = nbg_h2d(dn, h.nod, 16 * Nn, NULL);
+	if (rc == NBG_OK) rc = nbg_h2d(dc, h.conn, 4 * nen * Ne, NULL);
+	if (rc == NBG_OK) rc = nbg_h2d(du, displacement, 16 * Nn, NULL);
+	if (rc == NBG_OK) rc = nbg_strain_f64(nen, (uint32_t)Ne, dn, dc, du, ds, NULL);
+	if (rc == NBG_OK) rc = nbg_d2h(strain, ds, 8 * n3, NULL);
+	if (rc == NBG_OK) rc = nbg_stream_sync(NULL);
+	nbg_dev_free(dn);
+	nbg_dev_free(dc);
+	nbg_dev_free(du);
+	nbg_dev_free(ds);
+	free_problem(&h);
+	nbg_dropin_record_error(rc);
 }

@@ -248,6 +248,8 @@ void nbg_fem_destroy(nbg_fem_t *f)
 {
 	if (!f)
 		return;
+	if (f->borrowed_csr)
+		f->row_ptr = NULL, f->col_idx = NULL, f->K = NULL;
 	void *p[] = {f->nod, f->K, f->F, f->u, f->strain, f->stress, f->E, f->Ke, f->Fe, f->main_stress,
 		     f->damage,
 		     f->conn, f->row_ptr, f->col_idx, f->inc_ptr, f->inc_elem, f->distorted,
@@ -257,6 +259,72 @@ void nbg_fem_destroy(nbg_fem_t *f)
 	for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++)
 		nbg_dev_free(p[i]);
 	free(f);
+}
+
+int nbg_fem_create_on_csr(nbg_fem_t **out, const nbg_mesh_t *m, uint64_t nnz,
+			  uint32_t *row_ptr, uint32_t *col_idx, double *K, int need_incidence,
+			  void *stream)
+{
+	int rc = NBG_OK;
+	*out = NULL;
+	if (!m || (m->nen != 3 && m->nen != 4) || m->N_nod == 0)
+		return NBG_ERR_ARG;
+	nbg_fem_t *f = calloc(1, sizeof(*f));
+	if (!f)
+		return NBG_ERR_NOMEM;
+	f->m = *m;
+	f->m.nod = NULL;
+	f->m.conn = NULL;
+	f->m.edg = NULL;
+	f->stream = stream;
+	f->N = 2 * m->N_nod;
+	f->nnz = nnz;
+	f->row_ptr = row_ptr;
+	f->col_idx = col_idx;
+	f->K = K;
+	f->borrowed_csr = 1;
+	const size_t ne = m->N_elem, nen = m->nen, Nn = m->N_nod;
+	uint32_t *ip = NULL, *ie = NULL;
+	uint8_t *il = NULL;
+	TRY(nbg_dev_alloc((void **)&f->nod, 16 * Nn));
+	TRY(nbg_dev_alloc((void **)&f->conn, 4 * (ne ? ne : 1) * nen));
+	TRY(nbg_dev_alloc((void **)&f->F, 8 * (size_t)f->N));
+	TRY(nbg_dev_alloc((void **)&f->u, 8 * (size_t)f->N));
+	TRY(nbg_dev_alloc((void **)&f->E, 8 * (ne ? ne : 1)));
+	TRY(nbg_dev_alloc((void **)&f->enabled, ne ? ne : 1));
+	TRY(nbg_dev_alloc((void **)&f->strain, 8 * 3 * (ne ? ne : 1) * (nen == 4 ? 4 : 1)));
+	TRY(nbg_dev_alloc((void **)&f->stress, 8 * 3 * (ne ? ne : 1) * (nen == 4 ? 4 : 1)));
+	TRY(nbg_dev_alloc((void **)&f->distorted, 256));
+	TRY(nbg_dev_alloc((void **)&f->matched, 256));
+	TRY(nbg_dev_alloc((void **)&f->status, 256));
+	TRY(nbg_h2d(f->nod, m->nod, 16 * Nn, stream));
+	TRY(nbg_h2d(f->conn, m->conn, 4 * ne * nen, stream));
+	if (need_incidence) {
+		ip = malloc(4 * (Nn + 1));
+		ie = malloc(4 * (ne ? ne : 1) * nen);
+		il = malloc((ne ? ne : 1) * nen);
+		if (!ip || !ie || !il)
+			TRY(NBG_ERR_NOMEM);
+		TRY(nbg_host_incidence(m, ip, ie, il));
+		TRY(nbg_dev_alloc((void **)&f->inc_ptr, 4 * (Nn + 1)));
+		TRY(nbg_dev_alloc((void **)&f->inc_elem, 4 * (ne ? ne : 1) * nen));
+		TRY(nbg_dev_alloc((void **)&f->inc_local, (ne ? ne : 1) * nen));
+		TRY(nbg_h2d(f->inc_ptr, ip, 4 * (Nn + 1), stream));
+		TRY(nbg_h2d(f->inc_elem, ie, 4 * ne * nen, stream));
+		TRY(nbg_h2d(f->inc_local, il, ne * nen, stream));
+	}
+	TRY(nbg_stream_sync(stream));
+	free(ip);
+	free(ie);
+	free(il);
+	*out = f;
+	return NBG_OK;
+fail:
+	free(ip);
+	free(ie);
+	free(il);
+	nbg_fem_destroy(f);
+	return rc;
 }
 
 int nbg_fem_create(nbg_fem_t **out, const nbg_mesh_t *m, void *stream)
@@ -765,7 +833,15 @@ int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double n
 	TRY(nbg_fem_assemble_dev_damage(f, NULL, nu, thickness, 0.0, 0, g0, NULL, NULL));
 	TRY(nbg_fem_apply_bcs(f, bcs, 1.0));
 	TRY(zero_u(f));
-	TRY(solve_rhs(f, f->F, f->u, tol, method, &info->fwd_iters));
+	/* a solve that stops short of tol (status 1) still gives J and dJ */
+	int short_of_tol = 0;
+	{
+		int st = solve_rhs(f, f->F, f->u, tol, method, &info->fwd_iters);
+		if (st == NBG_NOT_CONVERGED)
+			short_of_tol = 1;
+		else
+			TRY(st);
+	}
 	TRY(nbg_d2h(hu, f->u, 8 * (size_t)N, f->stream));
 	TRY(nbg_d2h(hF, f->F, 8 * (size_t)N, f->stream));
 	TRY(nbg_stream_sync(f->stream));
@@ -787,13 +863,18 @@ int nbg_fem_simp(nbg_fem_t *f, const nbg_bcs_t *bcs, const double *rho, double n
 		}
 		TRY(nbg_h2d(f->simp_e, hF, 8 * (size_t)N, f->stream));
 		TRY(nbg_h2d(f->simp_lam, hu, 8 * (size_t)N, f->stream));
-		TRY(solve_rhs(f, f->simp_e, f->simp_lam, tol, method, &info->adj_iters));
+		int st = solve_rhs(f, f->simp_e, f->simp_lam, tol, method, &info->adj_iters);
+		if (st == NBG_NOT_CONVERGED)
+			short_of_tol = 1;
+		else
+			TRY(st);
 		adj = f->simp_lam;
 	}
 	TRY(nbg_simp_sensitivity_f64(f->m.nen, Ne, f->nod, f->conn, nu, thickness, f->simp_rho,
 				     penal, E0, Emin, adj, f->u, f->simp_out, f->stream));
 	TRY(nbg_d2h(dJ, f->simp_out, 8 * (size_t)Ne, f->stream));
 	TRY(nbg_stream_sync(f->stream));
+	rc = short_of_tol ? NBG_NOT_CONVERGED : NBG_OK;
 fail:
 	info->status = rc;
 	free(hu);

@@ -34,7 +34,18 @@ struct nbg_fem {
 	uint32_t block_sigma;      /* SELL-C-sigma window, 0: default */
 	uint32_t *perm, *iperm;    /* the block layout's node order, or NULL */
 	double *simp_rho, *simp_out, *simp_e, *simp_lam;  /* nbg_fem_simp buffers */
+	int borrowed_csr;          /* row_ptr, col_idx and K belong to the caller */
 };
+
+/* A FEM system on a CSR the caller owns on the device (row_ptr[N + 1],
+ * col_idx, values K; not freed by nbg_fem_destroy), N = 2 N_nod: the mesh
+ * arrays, F, u, strain and stress, and with need_incidence the node ->
+ * element incidence that assembly needs.  No block layout.  The gather
+ * assembly writes every pattern entry (those no element reaches get 0) and
+ * reports a missing element pair as NBG_ERR_PATTERN. */
+int nbg_fem_create_on_csr(nbg_fem_t **out, const nbg_mesh_t *m, uint64_t nnz,
+			  uint32_t *row_ptr, uint32_t *col_idx, double *K, int need_incidence,
+			  void *stream);
 
 /* Assembly with an optional device array of damage per Gauss point; E NULL
  * means the moduli are already in f->E. */

@@ -229,3 +229,14 @@ size_t nbg_solver_device_bytes(const nbg_solver_t *s)
 		     12 * (size_t)s->N;
 	return b;
 }
+
+int nbg_solver_block_layout(nbg_solver_t *s, nbg_bsr_t *out)
+{
+	if (!s->have_pattern)
+		return NBG_ERR_ARG;
+	if (!s->bsr_ok)
+		return NBG_ERR_PATTERN;
+	if (out)
+		*out = s->bsr;
+	return NBG_OK;
+}

@@ -34,7 +34,8 @@ class SimpProblem:
                                        self.p.nu, self.p.thickness, self.penal, self.E0,
                                        self.Emin, objective, dof, self.tol, self.method,
                                        dJ.ctypes.data, C.byref(info))
-        L.check(rc, "fem_simp")
+        if rc < 0:  # 1: a solve stopped short of tol (info.status), J and dJ still set
+            L.check(rc, "fem_simp")
         return info.J, dJ, info
 
     def close(self):

@@ -115,3 +115,84 @@ def test_fem_entry_known_answers(G):
     ob = NbotsObjects(p)
     st, u, strain = ob.fem()
     assert st == 0 and pwh_mean_vm_error(p, ob.stress(strain)) < PWH_MAX_VM_ERR
+
+
+@pytest.mark.parametrize("name", FEM_CASES)
+def test_pipeline_stages(G, name):
+    """An nbots program that drives the stages itself (static_elasticity2D.c:
+    31-81): nb_sparse_create on the nodal graph, pipeline_assemble_system,
+    nb_fem_set_bconditions, nb_sparse_solve_CG_precond_Jacobi (x0 = 0,
+    max_iter = N, 1e-8), pipeline_compute_strain, all through the drop-in.
+    K and F after each stage equal nbots' bit for bit, u is within 1e-10 of
+    nbots', and the strain of nbots' u is bit-exact."""
+    from nbots_gb300.dropin import NbotsObjects, csr_of, nodal_graph
+    p, d = load_golden(name)
+    ob = NbotsObjects(p)
+    g, keep = nodal_graph(p)
+    K = G.nb_sparse_create(C.byref(g), None, 2)
+    F = np.zeros(p.n_dof)
+    st = ob.pipeline(K, F)
+    assert st == int(d["assemble_status"][0])
+    if st:
+        G.nb_sparse_destroy(K)
+        ob.close()
+        return
+    rp, ci, vals = csr_of(K)
+    assert np.array_equal(rp, d["row_ptr"]) and np.array_equal(ci, d["col_idx"])
+    assert np.array_equal(vals.view(np.uint64), d["K_asm"].view(np.uint64))
+    assert np.array_equal(F.view(np.uint64), d["F_asm"].view(np.uint64))
+    ob.set_bconditions(K, F)
+    assert G.nbg_dropin_error() == 0
+    _, _, vals = csr_of(K)
+    assert np.array_equal(vals.view(np.uint64), d["K_bc"].view(np.uint64))
+    assert np.array_equal(F.view(np.uint64), d["F_bc"].view(np.uint64))
+    u = np.zeros(p.n_dof)
+    it, tr = C.c_uint32(0), C.c_double(0)
+    cst = G.nb_sparse_solve_CG_precond_Jacobi(K, F.ctypes.data, u.ctypes.data, p.n_dof, 1e-8,
+                                               C.byref(it), C.byref(tr), 1)
+    assert cst == int(d["cg_status"][0])
+    assert cg_iters_close(it.value, int(d["cg_niter"][0]), np.linalg.norm(F))
+    assert rel(u, d["u"]) < 1e-10
+    strain = ob.strain_of(d["u"])
+    assert G.nbg_dropin_error() == 0
+    assert np.array_equal(strain.view(np.uint64), d["strain"].view(np.uint64))
+    # the stages again on the same matrix (a second load case): nbots resets K
+    F2 = np.zeros(p.n_dof)
+    assert ob.pipeline(K, F2) == 0
+    _, _, vals = csr_of(K)
+    assert np.array_equal(vals.view(np.uint64), d["K_asm"].view(np.uint64))
+    G.nb_sparse_destroy(K)
+    ob.close()
+
+
+def test_device_copy_follows_host_writes(G):
+    """The matrix's device copy is reused while the matrix is unchanged and
+    re-sent after a write through any nb_sparse_* writer: each SpMV equals
+    nbots' on the current host values."""
+    from nbots_gb300.dropin import sparse_from_csr
+    from oracle import oracle as O
+    p, d = load_golden("c1_q4_64x32")
+    A, keep = sparse_from_csr(p, d["K_bc"])
+    x = np.ascontiguousarray(d["spmv_x"])
+    y = np.zeros(p.n_dof)
+    rp, ci = d["row_ptr"], d["col_idx"]
+
+    def check(K):
+        G.nb_sparse_multiply_vector(A, x.ctypes.data, y.ctypes.data, 1)
+        assert np.array_equal(y.view(np.uint64), O.spmv(rp, ci, K, x).view(np.uint64))
+    K = d["K_bc"].copy()
+    check(K)
+    check(K)                                    # the device copy, unchanged
+    G.nb_sparse_add(A, 0, int(ci[0]), 0.5)       # one write through the API
+    K[0] += 0.5
+    check(K)
+    G.nb_sparse_scale(A, 2.0)
+    K *= 2.0
+    check(K)
+    G.nb_sparse_reset(A)
+    check(np.zeros_like(K))
+    # a direct write to the rows, announced with nbg_dropin_sparse_touch
+    C.memmove(A.contents.rows_values[0], d["K_bc"].ctypes.data, d["K_bc"].nbytes)
+    G.nbg_dropin_sparse_touch(A)
+    check(d["K_bc"])
+    G.nb_sparse_destroy(A)

@@ -71,7 +71,8 @@ def test_lshape_assembly_and_solvers_on_gpu():
     assert A_sigma.perm and not A_mesh.perm
     assert A_sigma.n_entries < 0.8 * A_mesh.n_entries
     for sys_ in (s, m):
-        for solve, tol, slack, uerr in ((sys_.solve_fast, 1e-10, 2.0, 1e-7),
+        # both solvers judge convergence on the true FP64 residual
+        for solve, tol, slack, uerr in ((sys_.solve_fast, 1e-10, 1.01, 1e-7),
                                         (sys_.solve_mixed, 1e-11, 1.05, 1e-8)):
             res = solve(tol=tol)
             assert res.status == 0
