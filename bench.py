@@ -539,7 +539,8 @@ def bench_c3(args, with_cpu):
     N, nnz = s.N, s.nnz
     F = s.dptr(L.FEM_F)
     u = torch.zeros(N, dtype=torch.float64, device=dev)
-    ws_bytes = max(lib.nbg_cg_mixed_workspace_bytes(N), lib.nbg_cg_bsr_workspace_bytes(N))
+    ws_bytes = max(lib.nbg_cg_mixed_layout_workspace_bytes(C.byref(A)),
+                   lib.nbg_cg_bsr_workspace_bytes(N))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
 
@@ -717,7 +718,8 @@ def run_gpu(args):
     N, nnz = s.N, s.nnz
     F = s.dptr(L.FEM_F)
     u = torch.zeros(N, dtype=torch.float64, device=dev)
-    ws_bytes = max(lib.nbg_cg_mixed_workspace_bytes(N), lib.nbg_cg_bsr_workspace_bytes(N),
+    ws_bytes = max(lib.nbg_cg_mixed_layout_workspace_bytes(C.byref(A)),
+                   lib.nbg_cg_bsr_workspace_bytes(N),
                    lib.nbg_cg_workspace_bytes(N))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device=dev)
     flush = torch.empty(512 * 1024 * 1024 // 4, dtype=torch.float32, device=dev)
@@ -1052,7 +1054,8 @@ def run_profile(args):
     N = s.N
     F = s.dptr(L.FEM_F)
     u = torch.zeros(N, dtype=torch.float64, device="cuda")
-    ws_bytes = max(lib.nbg_cg_mixed_workspace_bytes(N), lib.nbg_cg_bsr_workspace_bytes(N))
+    ws_bytes = max(lib.nbg_cg_mixed_layout_workspace_bytes(C.byref(A)),
+                   lib.nbg_cg_bsr_workspace_bytes(N))
     ws = torch.empty(ws_bytes, dtype=torch.uint8, device="cuda")
     x64 = torch.randn(N, dtype=torch.float64, device="cuda")
     y64 = torch.empty_like(x64)

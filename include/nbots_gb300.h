@@ -268,8 +268,9 @@ int nbg_spmv_bsr_f32(const nbg_bsr_t *A, const float *x, float *y, void *stream)
  * recomputed in FP64 at that point, meets it too (else that residual
  * replaces the recurrence's and the iteration goes on); tol_reached is then
  * the true residual norm.  A target below the FP64 floor of the system (the
- * true residual stops falling between two such checks) ends the solve with
- * status 1 and that floor in tol_reached.  With NBG_CG_NBOTS_STOP: nbots' iteration and stop
+ * true residual stops falling between two such checks, or the recurrence
+ * does not meet the target again within k/8 iterations of a failed check)
+ * ends the solve with status 1 and that floor in tol_reached.  With NBG_CG_NBOTS_STOP: nbots' iteration and stop
  * test (the lagged ||g||, one iteration past the first ||g|| <= tol),
  * iterates within rounding of nbots' own.  NBG_CG_RELATIVE selects
  * ||g|| <= tol ||b||.  x holds x0 on entry. */
@@ -302,7 +303,17 @@ typedef struct {
 int nbg_spmv_bsr_mixed(const nbg_bsr_t *A, const float *ph, const float *pl, float *wh,
                        float *wl, void *stream);
 
+/* Workspace: nbg_cg_mixed_workspace_bytes(N) at least.  With
+ * nbg_cg_mixed_layout_workspace_bytes(A) (more: a 16-bit local column per
+ * layout entry and per-block ghost lists) the solver takes its ghost-node
+ * form when the system is small enough for each block's rows and ghosts to
+ * live in shared memory: every block keeps the search direction p of its
+ * own rows and of the rows its rows couple to (its ghosts) on chip, updates
+ * the ghosts itself from their owners' published residual, and so needs
+ * two grid barriers per iteration instead of three; the iterates are the
+ * same bit for bit.  ws NULL allocates the larger size. */
 size_t nbg_cg_mixed_workspace_bytes(uint32_t N);
+size_t nbg_cg_mixed_layout_workspace_bytes(const nbg_bsr_t *A);
 int nbg_cg_mixed(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_iter,
                  double tol, double delta, unsigned flags, nbg_mixed_result_t *result,
                  void *ws, size_t ws_bytes, void *stream);

@@ -24,9 +24,11 @@
 //    is still above the target, g replaces the recurrence's residual and the
 //    iteration continues with beta from the true g.q (residual replacement),
 //    so the reported norm is always a true FP64 residual.  A target below
-//    what FP64 can reach on the system shows as a second failed check with
-//    a true residual not even halved since the first: the solve then stops,
-//    not converged (status 1), reporting that floor.
+//    what FP64 can reach on the system shows either as a second failed check
+//    with a true residual not even halved since the first, or as a
+//    recurrence that does not meet the target again within k/8 (at least
+//    100) iterations of the failed check: the solve then stops, not
+//    converged (status 1), reporting the last true residual, that floor.
 // JAC = false is the unpreconditioned CG (q = g).
 #include <cstdint>
 
@@ -63,7 +65,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
     __shared__ int s_stop;     // 0 iterate, 1 stop, 2 confirm on the true residual first
     __shared__ struct {
         double gq, gq_old, gg, bb, target2, report, gg_check;
-        uint32_t k, checks;
+        uint32_t k, checks, k_check;
     } sc;  // scalar state, thread 0 only
     const unsigned G = gridDim.x;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -88,7 +90,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
 
     if (threadIdx.x == 0) {
         sc.gq = sc.gq_old = sc.gg = sc.bb = sc.target2 = sc.report = sc.gg_check = 0.0;
-        sc.k = sc.checks = 0;
+        sc.k = sc.checks = sc.k_check = 0;
     }
     {   // init: g = A x - b, q = g / Aii, p = -q
         double v[3] = {0.0, 0.0, 0.0};  // gq, gg, bb
@@ -189,6 +191,15 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
                 } else {
                     sc.gg = sc.report = t2[1];
                     s_stop = !(sc.gg > sc.target2) ? 2 : (sc.k >= a.max_iter ? 1 : 0);
+                    // after a failed check the recurrence gets k/8 (at least
+                    // 100) iterations to meet the target again; when it
+                    // hovers above it instead, the true residual of that
+                    // check is the FP64 floor
+                    if (s_stop == 0 && sc.checks > 0 &&
+                        sc.k - sc.k_check > max(sc.k_check / 8, 100u)) {
+                        s_stop = 1;
+                        sc.report = sc.gg_check;
+                    }
                 }
             }
             __syncthreads();
@@ -228,6 +239,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
                 // check): it sits at its FP64 floor above the target
                 const bool stalled = sc.checks > 1 && !(sc.gg < 0.25 * sc.gg_check);
                 sc.gg_check = sc.gg;
+                sc.k_check = sc.k;
                 s_stop = !(sc.gg > sc.target2) || stalled || sc.k >= a.max_iter ||
                          sc.checks >= 64;
             }

@@ -92,6 +92,12 @@ __device__ __forceinline__ uint2 ld_hint(const uint2* a, uint64_t pol) {
     return v;
 }
 
+__device__ __forceinline__ uint32_t ld_hint(const uint16_t* a, uint64_t pol) {
+    unsigned short v;
+    asm volatile("ld.global.L2::cache_hint.u16 %0, [%1], %2;" : "=h"(v) : "l"(a), "l"(pol));
+    return v;
+}
+
 __device__ __forceinline__ uint32_t ld_hint(const uint32_t* a, uint64_t pol) {
     uint32_t v;
     asm volatile("ld.global.L2::cache_hint.u32 %0, [%1], %2;" : "=r"(v) : "l"(a), "l"(pol));

@@ -542,12 +542,12 @@ __global__ void __launch_bounds__(kBatThreads, kBatMinBlocks)
 // 28 B per block entry) marked evict_last: what fits in NBG_L2_KEEP percent
 // of this device's L2, the rest of L2 being left to the gathered vector and
 // the other data.
-uint32_t keep_permille(const nbg_bsr_t& A) {
+uint32_t keep_permille(const nbg_bsr_t& A, double bytes_per_entry = 28.0) {
     int dev = 0, l2 = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess)
         return 0;
-    const double stream = 28.0 * (double)A.n_entries;
+    const double stream = bytes_per_entry * (double)A.n_entries;
     const double budget = l2 * (NBG_L2_KEEP / 100.0);
     if (stream <= 0.0 || budget >= stream) return 1000;
     return (uint32_t)(1000.0 * budget / stream);
@@ -584,6 +584,484 @@ __global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
     }
 }
 
+// ---------------------------------------------------------------------------
+// Ghost-node form of the single-system solver.
+//
+// A block's SpMV reads p at its own rows and at the rows of other blocks that
+// its rows couple to, its ghosts (on the 1M-dof cantilever, a block's strip of
+// about 3.4 grid rows has the two neighbouring grid rows as ghosts, 0.6 times
+// its own row count).  This form keeps p for the block's own rows and for
+// its ghosts in shared memory, with the layout's columns renumbered locally
+// in 16 bits (own row slots first, then the ghosts in ascending node order),
+// so the SpMV gathers from shared memory, not L2, and the matrix stream is
+// 26 B per block entry instead of 28.  Owners publish their FP32 residual r
+// (after L2 and after each reliable update); after the barrier that ends L2
+// every block computes its ghosts' new p itself, with the owner's arithmetic
+// on the owner's r and on its own copy of the ghost's previous p (the same
+// bits, by induction from p = z at the start), so the third barrier of each
+// iteration (the exchange of p) goes away.  The iterates equal those of the
+// global-gather form bit for bit.  x moves to global memory to leave shared
+// memory to the ghosts.
+//
+// The plan (ghost lists, local columns) depends on the launch's block
+// partition and is rebuilt by a short kernel at the start of every solve.
+constexpr uint32_t kGhostMax = 16384;   // ghosts per block
+constexpr uint32_t kGhostKeys = 32768;  // outside-column references per block the plan sorts
+
+struct GhostArgs {
+    const uint16_t* lcol;   // local column of every layout entry
+    const uint32_t* ids;    // kGhostMax ghost node ids per block, ascending
+    const uint32_t* count;  // ghosts per block
+    uint32_t scap;          // own row slots of the largest block
+    uint32_t pcap;          // row slots + ghosts, largest over the blocks
+    uint32_t gcap;          // ghosts, largest over the blocks
+};
+
+// One block per group of the solver's partition: its ghosts (the columns of
+// its live rows outside its row slots, sorted and made unique in shared
+// memory) and the local column of each of its entries.  *fail is set when a
+// block has more outside references than kGhostKeys, more ghosts than
+// kGhostMax, or more than 65535 local columns; the solver then keeps the
+// global-gather form.
+__global__ void __launch_bounds__(1024, 1) k_ghost_plan(nbg_bsr_t A, uint16_t* lcol,
+                                                      uint32_t* ids, uint32_t* count,
+                                                      int* fail) {
+    extern __shared__ __align__(16) uint32_t keys[];  // kGhostKeys
+    __shared__ uint32_t s_n;
+    __shared__ uint32_t s_scan[32];
+    const uint32_t tid = threadIdx.x, bd = blockDim.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t nw = bd >> 5;
+    uint32_t s0, s1;
+    slice_range(A.n_slices, s0, s1);
+    const uint32_t n0 = s0 * 32, nslot = (s1 - s0) * 32;
+    if (tid == 0) s_n = 0;
+    __syncthreads();
+    for (uint32_t s = s0 + warp; s < s1; s += nw) {
+        const uint32_t i = s * 32 + lane;
+        if (i >= A.Nn) continue;
+        for (uint32_t k = A.slice_off[s]; k < A.slice_off[s + 1]; k++) {
+            const uint32_t c = A.bcol[(size_t)k * 32 + lane];
+            if (c - n0 >= nslot) {
+                const uint32_t pos = atomicAdd(&s_n, 1u);
+                if (pos < kGhostKeys) keys[pos] = c;
+            }
+        }
+    }
+    __syncthreads();
+    const uint32_t n = s_n;
+    if (n > kGhostKeys) {  // the same n in every thread
+        if (tid == 0) atomicExch(fail, 1);
+        return;
+    }
+    uint32_t P2 = 1;
+    while (P2 < n) P2 <<= 1;
+    for (uint32_t j = n + tid; j < P2; j += bd) keys[j] = 0xffffffffu;
+    __syncthreads();
+    // bitonic sort of keys[0, P2)
+    for (uint32_t size = 2; size <= P2; size <<= 1)
+        for (uint32_t stride = size >> 1; stride > 0; stride >>= 1) {
+            for (uint32_t t = tid; t < P2 / 2; t += bd) {
+                const uint32_t lo = 2 * stride * (t / stride) + (t % stride), hi = lo + stride;
+                const uint32_t x = keys[lo], y = keys[hi];
+                if ((x > y) == ((lo & size) == 0)) {
+                    keys[lo] = y;
+                    keys[hi] = x;
+                }
+            }
+            __syncthreads();
+        }
+    // unique: each thread counts the first occurrences in its chunk, an
+    // exclusive block scan places them
+    const uint32_t chunk = (n + bd - 1) / bd;
+    const uint32_t j0 = min(tid * chunk, n), j1 = min(j0 + chunk, n);
+    uint32_t cnt = 0;
+    for (uint32_t j = j0; j < j1; j++) cnt += (j == 0 || keys[j] != keys[j - 1]);
+    uint32_t v = cnt;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        const uint32_t t = __shfl_up_sync(0xffffffffu, v, o);
+        if (lane >= (uint32_t)o) v += t;
+    }
+    if (lane == 31) s_scan[warp] = v;
+    __syncthreads();
+    if (warp == 0) {
+        uint32_t w = lane < nw ? s_scan[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            const uint32_t t = __shfl_up_sync(0xffffffffu, w, o);
+            if (lane >= (uint32_t)o) w += t;
+        }
+        s_scan[lane] = w;
+    }
+    __syncthreads();
+    const uint32_t u = s_scan[nw - 1];
+    if (u > kGhostMax || nslot + u > 65535u) {  // the same u in every thread
+        if (tid == 0) atomicExch(fail, 1);
+        return;
+    }
+    uint32_t* const my = ids + (size_t)blockIdx.x * kGhostMax;
+    uint32_t pos = v - cnt + (warp ? s_scan[warp - 1] : 0);
+    for (uint32_t j = j0; j < j1; j++)
+        if (j == 0 || keys[j] != keys[j - 1]) my[pos++] = keys[j];
+    __syncthreads();
+    for (uint32_t j = tid; j < u; j += bd) keys[j] = my[j];
+    if (tid == 0) count[blockIdx.x] = u;
+    __syncthreads();
+    for (uint32_t s = s0 + warp; s < s1; s += nw) {
+        const uint32_t i = s * 32 + lane;
+        for (uint32_t k = A.slice_off[s]; k < A.slice_off[s + 1]; k++) {
+            const size_t e = (size_t)k * 32 + lane;
+            uint32_t lc = i - n0;  // rows past Nn (never read): their own slot
+            if (i < A.Nn) {
+                const uint32_t c = A.bcol[e];
+                if (c - n0 < nslot) {
+                    lc = c - n0;
+                } else {
+                    uint32_t lo = 0, hi = u;  // first ghost >= c (it is there)
+                    while (lo < hi) {
+                        const uint32_t mid = (lo + hi) >> 1;
+                        if (keys[mid] < c) lo = mid + 1; else hi = mid;
+                    }
+                    lc = nslot + lo;
+                }
+            }
+            lcol[e] = (uint16_t)lc;
+        }
+    }
+}
+
+// spmv_half_split with local columns and p (own rows and ghosts) in shared
+// memory as float4 {hi of both dofs, lo of both dofs}; the same products and
+// sums in the same order.
+__device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t* __restrict__ lcol,
+                                                const float4* P, uint32_t s, uint32_t r,
+                                                uint32_t par, bool live, uint64_t pol, FF& y0,
+                                                FF& y1) {
+    const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
+    const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
+    FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
+    const uint32_t k0 = a.A.slice_off[s] + par, k1 = live ? a.A.slice_off[s + 1] : 0;
+#pragma unroll(kUnroll)
+    for (uint32_t k = k0; k < k1; k += 2) {
+        const size_t e = (size_t)k * 32 + r;
+        const uint32_t c = ld_hint(lcol + e, pol);
+        const float4 m = ld_hint(bh + e, pol);
+        const float4 sc = rem16_scale4(ld_hint(bl + e, pol));
+        const float4 pv = P[c];
+        c0.fma2s(m.x, sc.x, pv.x, pv.z);
+        c0.fma2s(m.y, sc.y, pv.y, pv.w);
+        c1.fma2s(m.z, sc.z, pv.x, pv.z);
+        c1.fma2s(m.w, sc.w, pv.y, pv.w);
+    }
+    FF t[2] = {c0.result(), c1.result()};
+#pragma unroll
+    for (int j = 0; j < 2; j++) {
+        const float h = __shfl_xor_sync(0xffffffffu, t[j].hi, 16);
+        const float l = __shfl_xor_sync(0xffffffffu, t[j].lo, 16);
+        t[j] = ff_add(t[j], FF{h, l});
+    }
+    y0 = t[0];
+    y1 = t[1];
+}
+
+// true_residual for the ghost form: r to shared memory and published to
+// global memory for the blocks that hold this row as a ghost.
+template <int kThreads>
+__device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float2* R, float4* P,
+                                                    uint32_t s0, uint32_t s1, double& rr,
+                                                    FFAcc& rz, double* bb, bool set_p) {
+    const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+    const uint32_t nw = kThreads / 32;
+    const double2* __restrict__ u = reinterpret_cast<const double2*>(a.u);
+    const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
+    const float2* __restrict__ dinv = reinterpret_cast<const float2*>(a.A.dinv32);
+    float2* __restrict__ gr = reinterpret_cast<float2*>(a.r);
+    for (uint32_t s = s0 + warp; s < s1; s += nw) {
+        const uint32_t i = s * 32 + lane, li = i - s0 * 32;
+        if (i >= a.A.Nn) continue;
+        const double2 au = spmv_row_f64(a.A, s, lane, u);
+        const double2 bi = b[i];
+        const double r0 = bi.x - au.x, r1 = bi.y - au.y;
+        rr = fma(r0, r0, fma(r1, r1, rr));
+        if (bb) *bb = fma(bi.x, bi.x, fma(bi.y, bi.y, *bb));
+        const float f0 = (float)r0, f1 = (float)r1;
+        R[li] = make_float2(f0, f1);
+        gr[i] = make_float2(f0, f1);
+        const float2 di = dinv[i];
+        const FF z0 = two_prod(f0, di.x), z1 = two_prod(f1, di.y);
+        rz.fma2(f0, 0.f, z0.hi, z0.lo);
+        rz.fma2(f1, 0.f, z1.hi, z1.lo);
+        if (set_p) P[li] = make_float4(z0.hi, z1.hi, z0.lo, z1.lo);
+    }
+}
+
+template <int kThreads>
+__device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group& g,
+                                                  const GhostArgs& gh, unsigned char* smem) {
+    __shared__ double red[3 * 32];
+    float2* const ffred = reinterpret_cast<float2*>(red);
+    __shared__ float s_alpha[2], s_beta[2];
+    __shared__ int s_flag;  // 0 iterate, 1 reliable update, 2 stop
+    __shared__ struct {
+        double rz, rmax2, rr64, bb, target2;
+        uint32_t k, nupd;
+        int converged;
+    } sc;  // scalar state, thread 0 only
+    const unsigned G = g.g_size;
+    const uint32_t rank = blockIdx.x - g.g_base;
+    const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+    const uint32_t nw = kThreads / 32;
+    uint32_t s0, s1;
+    group_slice_range(g.s_begin, g.s_end, rank, G, s0, s1);
+    const uint32_t Nn = a.A.Nn, nslot = (s1 - s0) * 32;
+    const uint32_t ng = gh.count[rank];
+    float4* const P = reinterpret_cast<float4*>(smem);
+    float2* const R = reinterpret_cast<float2*>(P + gh.pcap);
+    float2* const WH = R + gh.scap;
+    float2* const WL = WH + gh.scap;
+    uint32_t* const GID = reinterpret_cast<uint32_t*>(WL + gh.scap);
+    float2* __restrict__ gr = reinterpret_cast<float2*>(a.r);
+    float2* __restrict__ xh = reinterpret_cast<float2*>(a.xh);
+    float2* __restrict__ xl = reinterpret_cast<float2*>(a.xl);
+    const float2* __restrict__ dinv = reinterpret_cast<const float2*>(a.A.dinv32);
+    double* const part0 = g.part;
+    double* const part1 = g.part + g.pstride;
+    double* const part2 = g.part + 3 * g.pstride;
+    auto sync = [&]() { return grid_barrier(g.bar, G, rank, g.status); };
+
+    if (tid == 0) {
+        sc.rz = sc.rmax2 = sc.rr64 = sc.bb = sc.target2 = 0.0;
+        sc.k = sc.nupd = 0;
+        sc.converged = 0;
+    }
+    for (uint32_t j = tid; j < ng; j += kThreads) GID[j] = gh.ids[(size_t)rank * kGhostMax + j];
+    {   // init: x = 0, r = b - A u (FP64), own p = z, r published
+        for (uint32_t s = s0 + warp; s < s1; s += nw) {
+            const uint32_t i = s * 32 + lane;
+            if (i >= Nn) continue;
+            xh[i] = make_float2(0.f, 0.f);
+            xl[i] = make_float2(0.f, 0.f);
+        }
+        double rrl = 0.0, bbl = 0.0;
+        FFAcc rzk{0.f, 0.f};
+        true_residual_ghost<kThreads>(a, R, P, s0, s1, rrl, rzk, &bbl, true);
+        const FF t = rzk.result();
+        double v[3] = {rrl, bbl, (double)t.hi + (double)t.lo};
+        group_publish<3>(v, red, part2, rank);
+    }
+    if (sync()) goto done;
+    {
+        double t[3];
+        group_reduce0<3>(part2, G, t);
+        if (tid == 0) {
+            sc.rr64 = t[0];
+            sc.bb = t[1];
+            sc.rz = t[2];
+            sc.target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * sc.bb : a.tol * a.tol;
+            sc.rmax2 = sc.rr64;
+            sc.converged = !(sc.rr64 > sc.target2);
+            s_flag = (sc.converged || a.max_iter == 0) ? 2 : 0;
+        }
+        // ghosts start as their owners' p = z
+        for (uint32_t j = tid; j < ng; j += kThreads) {
+            const uint32_t c = GID[j];
+            const float2 rc = gr[c], dc = dinv[c];
+            const FF z0 = two_prod(rc.x, dc.x), z1 = two_prod(rc.y, dc.y);
+            P[nslot + j] = make_float4(z0.hi, z1.hi, z0.lo, z1.lo);
+        }
+        __syncthreads();
+    }
+    while (s_flag != 2) {
+        {   // L1: w = A p from shared memory, p.w (two lanes per node row)
+            FFAcc pw{0.f, 0.f};
+            const uint32_t par = lane >> 4, nh = 2 * (s1 - s0);
+            for (uint32_t h = warp; h < nh; h += nw) {
+                const uint32_t s = s0 + (h >> 1), r = ((h & 1) << 4) | (lane & 15);
+                const uint32_t i = s * 32 + r, li = i - s0 * 32;
+                if (s * 32 + ((h & 1) << 4) >= Nn) continue;
+                FF y0, y1;
+                const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
+                spmv_half_local(a, gh.lcol, P, s, r, par, i < Nn, pol, y0, y1);
+                if (par || i >= Nn) continue;
+                WH[li] = make_float2(y0.hi, y1.hi);
+                WL[li] = make_float2(y0.lo, y1.lo);
+                const float4 p = P[li];
+                pw.fma2(p.x, p.z, y0.hi, y0.lo);
+                pw.fma2(p.y, p.w, y1.hi, y1.lo);
+            }
+            FF v[1] = {pw.result()};
+            group_publish_ff<1>(v, ffred, reinterpret_cast<float2*>(part0), rank);
+        }
+        if (sync()) goto done;
+        {
+            double pwd[1];
+            group_reduce0_ff<1>(reinterpret_cast<const float2*>(part0), G, pwd);
+            if (tid == 0) {
+                const FF al = ff_from_double(sc.rz / pwd[0]);
+                s_alpha[0] = al.hi;
+                s_alpha[1] = al.lo;
+            }
+            __syncthreads();
+        }
+        {   // L2: x += alpha p, r -= alpha w, z = r / Aii; r published
+            const FF alpha = {s_alpha[0], s_alpha[1]};
+            FFAcc rzk{0.f, 0.f}, rrk{0.f, 0.f};
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane, li = i - s0 * 32;
+                if (i >= Nn) continue;
+                const float4 p = P[li];
+                const float2 w = WH[li], wlo = WL[li];
+                const float2 xhi = xh[i], xlo = xl[i];
+                const float2 ri = R[li], di = dinv[i];
+                const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, p.z}));
+                const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, p.w}));
+                xh[i] = make_float2(x0.hi, x1.hi);
+                xl[i] = make_float2(x0.lo, x1.lo);
+                const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
+                const FF t0 = two_sum(ri.x, -aw0.hi), t1 = two_sum(ri.y, -aw1.hi);
+                const float r0 = __fadd_rn(t0.hi, __fsub_rn(t0.lo, aw0.lo));
+                const float r1 = __fadd_rn(t1.hi, __fsub_rn(t1.lo, aw1.lo));
+                R[li] = make_float2(r0, r1);
+                gr[i] = make_float2(r0, r1);
+                const FF z0 = two_prod(r0, di.x), z1 = two_prod(r1, di.y);
+                rzk.fma2(r0, 0.f, z0.hi, z0.lo);
+                rzk.fma2(r1, 0.f, z1.hi, z1.lo);
+                rrk.fma2(r0, 0.f, r0, 0.f);
+                rrk.fma2(r1, 0.f, r1, 0.f);
+            }
+            FF v[2] = {rzk.result(), rrk.result()};
+            group_publish_ff<2>(v, ffred, reinterpret_cast<float2*>(part1), rank);
+        }
+        if (sync()) goto done;
+        {
+            double t2[2];
+            group_reduce0_ff<2>(reinterpret_cast<const float2*>(part1), G, t2);
+            if (tid == 0) {
+                const double rz_new = t2[0], rr = t2[1];
+                if (rr > sc.rmax2) sc.rmax2 = rr;
+                sc.k++;
+                const int upd = rr <= a.delta * a.delta * sc.rmax2 || rr <= sc.target2 ||
+                                sc.k >= a.max_iter;
+                if (!upd) {
+                    const FF be = ff_from_double(rz_new / sc.rz);
+                    sc.rz = rz_new;
+                    s_beta[0] = be.hi;
+                    s_beta[1] = be.lo;
+                }
+                s_flag = upd;
+            }
+            __syncthreads();
+        }
+        if (s_flag) {
+            // reliable update: u += x in FP64, then r = b - A u in FP64
+            double2* __restrict__ u = reinterpret_cast<double2*>(a.u);
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane;
+                if (i >= Nn) continue;
+                const float2 xhi = xh[i], xlo = xl[i];
+                double2 ui = u[i];
+                ui.x += (double)xhi.x + (double)xlo.x;
+                ui.y += (double)xhi.y + (double)xlo.y;
+                u[i] = ui;
+                xh[i] = make_float2(0.f, 0.f);
+                xl[i] = make_float2(0.f, 0.f);
+            }
+            if (sync()) goto done;
+            double rrl = 0.0;
+            FFAcc rzk{0.f, 0.f};
+            true_residual_ghost<kThreads>(a, R, P, s0, s1, rrl, rzk, nullptr, false);
+            const FF t = rzk.result();
+            double v[2] = {rrl, (double)t.hi + (double)t.lo};
+            group_publish<2>(v, red, part2, rank);
+            if (sync()) goto done;
+            double tt[2];
+            group_reduce0<2>(part2, G, tt);
+            if (tid == 0) {
+                sc.rr64 = tt[0];
+                sc.rmax2 = sc.rr64;
+                sc.nupd++;
+                sc.converged = !(sc.rr64 > sc.target2);
+                const int stop = sc.converged || sc.k >= a.max_iter;
+                if (!stop) {
+                    const FF be = ff_from_double(tt[1] / sc.rz);
+                    sc.rz = tt[1];
+                    s_beta[0] = be.hi;
+                    s_beta[1] = be.lo;
+                }
+                s_flag = stop ? 2 : 0;
+            }
+            __syncthreads();
+            if (s_flag == 2) break;
+        }
+        {   // L3: p = z + beta p for the own rows and the ghosts (no barrier:
+            // every p this block's next SpMV reads is in its shared memory)
+            const FF beta = {s_beta[0], s_beta[1]};
+            for (uint32_t s = s0 + warp; s < s1; s += nw) {
+                const uint32_t i = s * 32 + lane, li = i - s0 * 32;
+                if (i >= Nn) continue;
+                const float2 ri = R[li], di = dinv[i];
+                const float4 p = P[li];
+                const FF n0 = ff_add(two_prod(ri.x, di.x), ff_mul(beta, {p.x, p.z}));
+                const FF n1 = ff_add(two_prod(ri.y, di.y), ff_mul(beta, {p.y, p.w}));
+                P[li] = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
+            }
+            for (uint32_t j = tid; j < ng; j += kThreads) {
+                const uint32_t c = GID[j];
+                const float2 rc = gr[c], dc = dinv[c];
+                const float4 p = P[nslot + j];
+                const FF n0 = ff_add(two_prod(rc.x, dc.x), ff_mul(beta, {p.x, p.z}));
+                const FF n1 = ff_add(two_prod(rc.y, dc.y), ff_mul(beta, {p.y, p.w}));
+                P[nslot + j] = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
+            }
+            __syncthreads();
+        }
+    }
+    {   // b.u in FP64 (the compliance F^T u when b is the load vector).  part0
+        // was last read before the L2 barrier of the last iteration.
+        const double2* __restrict__ u = reinterpret_cast<const double2*>(a.u);
+        const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
+        double bu = 0.0;
+        for (uint32_t s = s0 + warp; s < s1; s += nw) {
+            const uint32_t i = s * 32 + lane;
+            if (i >= Nn) continue;
+            const double2 ui = u[i], bi = b[i];
+            bu = fma(bi.x, ui.x, fma(bi.y, ui.y, bu));
+        }
+        double v[1] = {bu};
+        group_publish<1>(v, red, part0, rank);
+        if (sync()) goto done;
+        double J[1];
+        group_reduce0<1>(part0, G, J);
+        if (rank == 0 && tid == 0) g.res[5] = J[0];
+    }
+done:
+    if (rank == 0 && tid == 0) {
+        g.res[0] = (double)sc.k;
+        g.res[1] = (double)sc.nupd;
+        int st = ld_volatile(g.status);
+        g.res[2] = st != 0 ? (double)st : (sc.converged ? 0.0 : 1.0);
+        g.res[3] = sc.rr64;
+        g.res[4] = sc.bb;
+    }
+}
+
+__global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
+    k_cg_mixed_ghost(MixArgs a, Group g, GhostArgs gh) {
+    extern __shared__ __align__(16) unsigned char smem[];
+    mixed_solve_ghost<kMixThreads>(a, g, gh, smem);
+}
+
+// Workspace of the ghost plan for layout A on this device: local columns,
+// ghost lists of up to one block per SM, counts, the failure flag.
+size_t ghost_plan_bytes(const nbg_bsr_t& A) {
+    int dev = 0, nsm = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+        return 0;
+    const size_t G = (size_t)nsm * kMixMinBlocks;
+    return align256(2 * (size_t)A.n_entries) + align256(G * kGhostMax * 4) + align256(G * 4) + 256;
+}
+
 }  // namespace
 
 extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const float* pl,
@@ -611,6 +1089,76 @@ extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const flo
 
 extern "C" size_t nbg_cg_mixed_workspace_bytes(uint32_t N) { return mixed_bytes(N); }
 
+extern "C" size_t nbg_cg_mixed_layout_workspace_bytes(const nbg_bsr_t* A) {
+    return A ? mixed_bytes(A->N) + ghost_plan_bytes(*A) : 0;
+}
+
+namespace {
+// The ghost plan for a G-block partition of A, and the launch data of the
+// ghost form when its vectors fit in shared memory at one block per SM:
+// returns 1 and fills gh and *dyn, or 0 (the caller keeps the global-gather
+// form).  plan: the workspace region of ghost_plan_bytes(A).
+int ghost_setup(const nbg_bsr_t& A, unsigned G, char* plan, cudaStream_t s, GhostArgs* gh,
+                size_t* dyn) {
+    if (!NBG_MIXED_RESIDENT || sizeof(LoP::one) != 4 || sizeof(LoW::one) != 4) return 0;
+    uint16_t* lcol = (uint16_t*)plan;
+    uint32_t* ids = (uint32_t*)(plan + align256(2 * (size_t)A.n_entries));
+    uint32_t* count = ids + (size_t)G * kGhostMax;
+    int* fail = (int*)((char*)count + align256((size_t)G * 4));
+    int dev = 0, nsm = 0, optin = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev) !=
+            cudaSuccess)
+        return 0;
+    if (G > (unsigned)nsm * kMixMinBlocks) return 0;  // beyond the plan's space
+    if (cudaFuncSetAttribute((const void*)k_ghost_plan,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(kGhostKeys * 4)) != cudaSuccess)
+        return 0;
+    if (cudaMemsetAsync(fail, 0, sizeof(int), s) != cudaSuccess) return 0;
+    k_ghost_plan<<<G, 1024, kGhostKeys * 4, s>>>(A, lcol, ids, count, fail);
+    if (cudaGetLastError() != cudaSuccess) return 0;
+    std::vector<uint32_t> cnt(G);
+    int hfail = 1;
+    if (cudaMemcpyAsync(cnt.data(), count, 4 * (size_t)G, cudaMemcpyDeviceToHost, s) !=
+            cudaSuccess ||
+        cudaMemcpyAsync(&hfail, fail, sizeof(int), cudaMemcpyDeviceToHost, s) != cudaSuccess ||
+        cudaStreamSynchronize(s) != cudaSuccess || hfail)
+        return 0;
+    uint32_t scap = 0, pcap = 0, gcap = 0;
+    for (unsigned b = 0; b < G; b++) {
+        const uint32_t s0 = (uint32_t)(((uint64_t)A.n_slices * b) / G);
+        const uint32_t s1 = (uint32_t)(((uint64_t)A.n_slices * (b + 1)) / G);
+        scap = std::max(scap, 32 * (s1 - s0));
+        pcap = std::max(pcap, 32 * (s1 - s0) + cnt[b]);
+        gcap = std::max(gcap, cnt[b]);
+    }
+    const size_t bytes = 16 * (size_t)pcap + 24 * (size_t)scap + 4 * (size_t)gcap;
+    cudaFuncAttributes fa;
+    if (cudaFuncGetAttributes(&fa, (const void*)k_cg_mixed_ghost) != cudaSuccess ||
+        bytes + fa.sharedSizeBytes > (size_t)optin)
+        return 0;
+    if (cudaFuncSetAttribute((const void*)k_cg_mixed_ghost,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes) !=
+        cudaSuccess)
+        return 0;
+    int occ = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&occ, (const void*)k_cg_mixed_ghost,
+                                                      kMixThreads, bytes) != cudaSuccess ||
+        (unsigned)occ * (unsigned)nsm < G)
+        return 0;
+    gh->lcol = lcol;
+    gh->ids = ids;
+    gh->count = count;
+    gh->scap = scap;
+    gh->pcap = pcap;
+    gh->gcap = gcap;
+    *dyn = bytes;
+    return 1;
+}
+}  // namespace
+
 extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint32_t max_iter,
                             double tol, double delta, unsigned flags, nbg_mixed_result_t* result,
                             void* ws, size_t ws_bytes, void* stream) {
@@ -620,15 +1168,18 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     if (!A->b64 || !A->b32 || !A->blo || !A->dinv32 || !(delta > 0.0 && delta < 1.0))
         return NBG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
-    const size_t need = mixed_bytes(A->N);
+    const size_t need = mixed_bytes(A->N), plan_bytes = ghost_plan_bytes(*A);
     void* own = nullptr;
     if (!ws) {
-        NBG_CHECK(cudaMalloc(&own, need));
+        NBG_CHECK(cudaMalloc(&own, need + plan_bytes));
         ws = own;
+        ws_bytes = need + plan_bytes;
     } else if (ws_bytes < need) {
         return NBG_ERR_ARG;
     }
     char* base = (char*)ws;
+    // the ghost form when the workspace holds its plan
+    char* const plan = plan_bytes && ws_bytes >= need + plan_bytes ? base + need : nullptr;
     const size_t f = align256((size_t)A->N * 4), h = align256((size_t)A->N * 4);
     MixArgs a;
     a.A = *A;
@@ -665,21 +1216,38 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
         a.b = bp;
         a.u = xp;
     }
-    if (e == cudaSuccess)
+    GhostArgs gh;
+    memset(&gh, 0, sizeof(gh));
+    bool ghost = false;
+    if (e == cudaSuccess && plan) {
+        // one block per SM, as the resident global-gather form's first choice
+        int dev = 0, nsm = 0;
+        if (cudaGetDevice(&dev) == cudaSuccess &&
+            cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev) == cudaSuccess) {
+            const unsigned want = (A->n_slices + kMixThreads / 32 - 1) / (kMixThreads / 32);
+            G = std::max(1u, std::min((unsigned)nsm * kMixMinBlocks, want));
+            ghost = ghost_setup(*A, G, plan, s, &gh, &dyn) == 1;
+        }
+        (void)cudaGetLastError();  // a plan that could not run leaves the global-gather form
+    }
+    if (e == cudaSuccess && !ghost)
         rc = coop_grid_resident((const void*)k_cg_mixed<true>, A->n_slices,
                                 NBG_MIXED_RESIDENT ? kOwnNodeBytes * 32 : 0, &G, &dyn, kMixThreads,
                                 kMixMinBlocks);
-    if (e == cudaSuccess && rc == NBG_OK && dyn == 0)
+    if (e == cudaSuccess && rc == NBG_OK && !ghost && dyn == 0)
         rc = coop_grid((const void*)k_cg_mixed<false>, A->n_slices, &G, kMixThreads);
     a.resident = dyn > 0;
-    const void* fn = a.resident ? (const void*)k_cg_mixed<true> : (const void*)k_cg_mixed<false>;
+    const void* fn = ghost ? (const void*)k_cg_mixed_ghost
+                           : a.resident ? (const void*)k_cg_mixed<true>
+                                        : (const void*)k_cg_mixed<false>;
     g.s_begin = 0;
     g.s_end = A->n_slices;
     g.g_base = 0;
     g.g_size = G;
     g.pstride = kMaxBlocks;
+    if (ghost) a.keep_pm = keep_permille(*A, 26.0);
     if (e == cudaSuccess && rc == NBG_OK) {
-        void* args[] = {&a, &g};
+        void* args[] = {&a, &g, &gh};
         e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kMixThreads),
                                         args, dyn, s);
         if (e == cudaSuccess && A->perm) e = perm_scatter(A->Nn, A->perm, (const double*)a.u, x, s);

@@ -698,7 +698,7 @@ int nbg_fem_solve_mixed(nbg_fem_t *f, uint32_t max_iter, double tol, double delt
 {
 	int rc = NBG_OK;
 	TRY(nbg_fem_block_layout(f, NULL));
-	TRY(ensure_ws(f, nbg_cg_mixed_workspace_bytes(f->N)));
+	TRY(ensure_ws(f, nbg_cg_mixed_layout_workspace_bytes(&f->bsr)));
 	TRY(zero_u(f));
 	return nbg_cg_mixed(&f->bsr, f->F, f->u, max_iter, tol, delta, flags, res, f->cg_ws,
 			    f->cg_ws_bytes, f->stream);
@@ -791,7 +791,7 @@ static int solve_rhs(nbg_fem_t *f, const double *b, double *x, double tol, int m
 	int rc = nbg_fem_block_layout(f, NULL);
 	if (rc != NBG_OK)
 		return rc;
-	const size_t need = method == NBG_METHOD_MIXED ? nbg_cg_mixed_workspace_bytes(f->N)
+	const size_t need = method == NBG_METHOD_MIXED ? nbg_cg_mixed_layout_workspace_bytes(&f->bsr)
 						      : nbg_cg_bsr_workspace_bytes(f->N);
 	if ((rc = ensure_ws(f, need)) != NBG_OK)
 		return rc;

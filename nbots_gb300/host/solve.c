@@ -137,7 +137,7 @@ int nbg_solver_solve(nbg_solver_t *s, const double *b, double *x, uint32_t max_i
 	if (method != NBG_METHOD_NBOTS && !s->bsr_ok)
 		return NBG_ERR_PATTERN;
 	size_t need = method == NBG_METHOD_NBOTS ? nbg_cg_workspace_bytes(s->N)
-		    : method == NBG_METHOD_MIXED ? nbg_cg_mixed_workspace_bytes(s->N)
+		    : method == NBG_METHOD_MIXED ? nbg_cg_mixed_layout_workspace_bytes(&s->bsr)
 		    : nbg_cg_bsr_workspace_bytes(s->N);
 	if (s->ws_bytes < need) {
 		nbg_dev_free(s->ws);

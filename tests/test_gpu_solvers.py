@@ -149,3 +149,56 @@ def test_bounded_device_wait_times_out_and_context_survives(L):
     # the context is still usable
     p, d, s = system("q4_allbc_16x8")
     assert s.solve().status == 0
+
+
+def mixed_on(L, A, F, N, ws_bytes, tol=1e-10):
+    from nbots_gb300.device import DeviceArray
+    lib = L.lib()
+    u = DeviceArray(np.zeros(N))
+    ws = DeviceArray(shape=(max(ws_bytes, 1),), dtype=np.uint8)
+    r = L.MixedResult()
+    rc = lib.nbg_cg_mixed(C.byref(A), F, u.ptr, 8 * N, tol, 0.1, L.CG_JACOBI | L.CG_RELATIVE,
+                          C.byref(r), ws.ptr, ws_bytes, None)
+    return rc, r, u.numpy()
+
+
+@pytest.mark.parametrize("name", ["c1_q4_64x32", "q4_lognormal_32x16"])
+def test_mixed_ghost_form_equals_global_gather_form(L, name):
+    """With the layout-sized workspace the mixed solver keeps each block's
+    ghosts in shared memory (two grid barriers per iteration); with the
+    minimal one it gathers p from global memory (three).  The iterates, and
+    so the iteration count and the solution, are the same bit for bit."""
+    p, d, s = system(name)
+    A = s.block_layout()
+    lib = L.lib()
+    N, F = s.N, s.dptr(L.FEM_F)
+    small = lib.nbg_cg_mixed_workspace_bytes(N)
+    full = lib.nbg_cg_mixed_layout_workspace_bytes(C.byref(A))
+    assert full > small
+    rc0, r0, u0 = mixed_on(L, A, F, N, small)
+    rc1, r1, u1 = mixed_on(L, A, F, N, full)
+    assert rc0 == rc1 == 0
+    assert (r1.niter, r1.n_updates) == (r0.niter, r0.n_updates)
+    assert np.array_equal(u1.view(np.uint64), u0.view(np.uint64))
+    assert true_relres(d, u1) <= 1.05e-10
+    s.close()
+
+
+def test_mixed_ghost_form_full_size_bit_identical(L):
+    """The same on the 1M-dof cantilever, where each of the 152 blocks holds
+    about 3,500 own node rows and 2,000 ghosts."""
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.fem import FemSystem
+    s = FemSystem(W.config_c2())
+    assert s.assemble() == 0
+    s.apply_bcs()
+    A = s.block_layout()
+    lib = L.lib()
+    N, F = s.N, s.dptr(L.FEM_F)
+    rc0, r0, u0 = mixed_on(L, A, F, N, lib.nbg_cg_mixed_workspace_bytes(N), tol=1e-8)
+    rc1, r1, u1 = mixed_on(L, A, F, N, lib.nbg_cg_mixed_layout_workspace_bytes(C.byref(A)),
+                           tol=1e-8)
+    assert rc0 == rc1 == 0
+    assert (r1.niter, r1.n_updates) == (r0.niter, r0.n_updates)
+    assert np.array_equal(u1.view(np.uint64), u0.view(np.uint64))
+    s.close()
