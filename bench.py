@@ -448,8 +448,8 @@ def bench_c5(args, lib, L, W, sp, dev, stream, flush, share=None):
     Fd = lib.nbg_fem_device_ptr(b.fem, L.FEM_F)
     rc = lib.nbg_cg_bsr_f64(C.byref(A), Fd, u64.data_ptr(), 200000, 1e-13,
                             L.CG_JACOBI | L.CG_RELATIVE, C.byref(r64), ws.data_ptr(), wsb, sp)
-    # relres 1e-13, or the FP64 floor of the merged system just above it
-    assert rc == 0 or (rc == 1 and r64.tol_reached <= 1e-11 * r64.bnorm), rc
+    # relres 1e-13, or the FP64 floor of the merged system (below 1e-10)
+    assert rc == 0 or (rc == 1 and r64.tol_reached <= 1e-10 * r64.bnorm), rc
     rho_d = torch.from_numpy(np.concatenate(rho)).to(dev)
     g64 = torch.empty(b.n_elems, dtype=torch.float64, device=dev)
     L.check(lib.nbg_simp_sensitivity_f64(4, b.n_elems, lib.nbg_fem_device_ptr(b.fem, L.FEM_NOD),

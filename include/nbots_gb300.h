@@ -269,7 +269,8 @@ int nbg_spmv_bsr_f32(const nbg_bsr_t *A, const float *x, float *y, void *stream)
  * replaces the recurrence's and the iteration goes on); tol_reached is then
  * the true residual norm.  A target below the FP64 floor of the system (the
  * true residual stops falling between two such checks, or the recurrence
- * does not meet the target again within k/8 iterations of a failed check)
+ * does not meet the target again within twice the iterations its rate so
+ * far needs)
  * ends the solve with status 1 and that floor in tol_reached.  With NBG_CG_NBOTS_STOP: nbots' iteration and stop
  * test (the lagged ||g||, one iteration past the first ||g|| <= tol),
  * iterates within rounding of nbots' own.  NBG_CG_RELATIVE selects

@@ -26,8 +26,8 @@
 //    so the reported norm is always a true FP64 residual.  A target below
 //    what FP64 can reach on the system shows either as a second failed check
 //    with a true residual not even halved since the first, or as a
-//    recurrence that does not meet the target again within k/8 (at least
-//    100) iterations of the failed check: the solve then stops, not
+//    recurrence that does not meet the target again within twice the
+//    iterations its rate so far needs (plus 100): the solve then stops, not
 //    converged (status 1), reporting the last true residual, that floor.
 // JAC = false is the unpreconditioned CG (q = g).
 #include <cstdint>
@@ -64,8 +64,8 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
     __shared__ double s_coef;  // alpha, then beta
     __shared__ int s_stop;     // 0 iterate, 1 stop, 2 confirm on the true residual first
     __shared__ struct {
-        double gq, gq_old, gg, bb, target2, report, gg_check;
-        uint32_t k, checks, k_check;
+        double gq, gq_old, gg, bb, target2, report, gg_check, gg0, k_limit;
+        uint32_t k, checks;
     } sc;  // scalar state, thread 0 only
     const unsigned G = gridDim.x;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -90,7 +90,8 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
 
     if (threadIdx.x == 0) {
         sc.gq = sc.gq_old = sc.gg = sc.bb = sc.target2 = sc.report = sc.gg_check = 0.0;
-        sc.k = sc.checks = sc.k_check = 0;
+        sc.gg0 = sc.k_limit = 0.0;
+        sc.k = sc.checks = 0;
     }
     {   // init: g = A x - b, q = g / Aii, p = -q
         double v[3] = {0.0, 0.0, 0.0};  // gq, gg, bb
@@ -119,7 +120,7 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
         group_reduce0<3>(part2, G, t);
         if (threadIdx.x == 0) {
             sc.gq = t[0];
-            sc.gg = sc.report = t[1];
+            sc.gg = sc.report = sc.gg0 = t[1];
             sc.bb = t[2];
             sc.target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * sc.bb : a.tol * a.tol;
             s_stop = !(sc.gg > sc.target2) || a.max_iter == 0;
@@ -191,12 +192,11 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
                 } else {
                     sc.gg = sc.report = t2[1];
                     s_stop = !(sc.gg > sc.target2) ? 2 : (sc.k >= a.max_iter ? 1 : 0);
-                    // after a failed check the recurrence gets k/8 (at least
-                    // 100) iterations to meet the target again; when it
-                    // hovers above it instead, the true residual of that
-                    // check is the FP64 floor
-                    if (s_stop == 0 && sc.checks > 0 &&
-                        sc.k - sc.k_check > max(sc.k_check / 8, 100u)) {
+                    // after a failed check the recurrence gets twice the
+                    // iterations its rate so far needs to meet the target
+                    // again; when it hovers above it instead, the true
+                    // residual of that check is the FP64 floor
+                    if (s_stop == 0 && sc.checks > 0 && (double)sc.k > sc.k_limit) {
                         s_stop = 1;
                         sc.report = sc.gg_check;
                     }
@@ -239,7 +239,11 @@ __global__ void __launch_bounds__(kPersistThreads, kPersistMinBlocks) k_cg_bsr_f
                 // check): it sits at its FP64 floor above the target
                 const bool stalled = sc.checks > 1 && !(sc.gg < 0.25 * sc.gg_check);
                 sc.gg_check = sc.gg;
-                sc.k_check = sc.k;
+                // iterations to go from this residual to the target at the
+                // rate of the k so far (from gg0 to the target)
+                const double need = (double)sc.k * log(sc.gg / sc.target2) /
+                                    log(sc.gg0 / sc.target2);
+                sc.k_limit = (double)sc.k + 2.0 * need + 100.0;
                 s_stop = !(sc.gg > sc.target2) || stalled || sc.k >= a.max_iter ||
                          sc.checks >= 64;
             }

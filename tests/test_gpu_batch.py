@@ -39,8 +39,9 @@ def batch(L):
 
 def converged_fp64(r):
     """An FP64 reference solve: relres 1e-13, or stopped at the system's FP64
-    floor (status 1 with a true residual below 1e-11 ||F||)."""
-    return r.status == 0 or (r.status == 1 and r.tol_reached <= 1e-11 * r.bnorm)
+    floor (status 1 with a true residual below 1e-10 ||F||, a hundred
+    times below the tolerances compared against it)."""
+    return r.status == 0 or (r.status == 1 and r.tol_reached <= 1e-10 * r.bnorm)
 
 
 def single(L, p, E):
@@ -87,7 +88,8 @@ def test_batched_solve_matches_fp64(L, batch):
     for k, p in enumerate(probs):
         assert res[k].status == 0 and res[k].relres <= 1e-10, k
         s = single(L, p, E[int(b.elem_off[k]):int(b.elem_off[k + 1])].copy())
-        assert converged_fp64(s.solve_fast(tol=1e-13))
+        r64 = s.solve_fast(tol=1e-13)
+        assert converged_fp64(r64), (r64.status, r64.niter, r64.tol_reached / r64.bnorm)
         u64 = s.get(L.FEM_U)
         F = s.get(L.FEM_F)
         err = np.linalg.norm(us[k] - u64) / np.linalg.norm(u64)
@@ -164,7 +166,8 @@ def test_t3_batch(L):
         assert np.array_equal(ci[seg] - no, s.get(L.FEM_COL_IDX))
         assert np.array_equal(K[seg].view(np.uint64), s.get(L.FEM_K).view(np.uint64))
         assert res[k].status == 0 and res[k].relres <= 1e-10, k
-        assert converged_fp64(s.solve_fast(tol=1e-13))
+        r64 = s.solve_fast(tol=1e-13)
+        assert converged_fp64(r64), (r64.status, r64.niter, r64.tol_reached / r64.bnorm)
         u64 = s.get(L.FEM_U)
         assert np.linalg.norm(us[k] - u64) / np.linalg.norm(u64) < 1e-8, k
         s.close()
