@@ -99,6 +99,29 @@ class Clocks:
 
 
 # ------------------------------------------------------------------ CPU
+def mixed_blocks(n_slices, dev):
+    """Blocks of the single-system mixed launch: one per SM, at most one per
+    32 slices (the solver's own rule)."""
+    import torch
+    nsm = torch.cuda.get_device_properties(dev).multi_processor_count
+    return max(1, min(nsm, (n_slices + 31) // 32))
+
+
+def ghost_count(rp, ci, n_slices, G):
+    """Ghost node rows over all blocks of a G-block partition of the slices
+    (what the solver's plan finds): per block, the distinct column nodes of
+    its rows outside its own row slots."""
+    rows = np.repeat(np.arange(rp.shape[0] - 1, dtype=np.int64) // 2,
+                     np.diff(rp).astype(np.int64))
+    cols = ci.astype(np.int64) // 2
+    s_of_block = (n_slices * np.arange(G + 1, dtype=np.int64)) // G
+    blk = np.searchsorted(s_of_block, rows // 32, side="right") - 1
+    lo, hi = 32 * s_of_block[blk], 32 * s_of_block[blk + 1]
+    out = (cols < lo) | (cols >= hi)
+    key = blk[out] * (int(cols.max()) + 1) + cols[out]
+    return int(np.unique(key).size)
+
+
 def cpu_model():
     try:
         out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
@@ -262,22 +285,25 @@ def bench_damage(L, W, with_cpu):
     cantilever under a uniform top traction: 4 load steps, at most 40
     iterations each, 6 without a new best residual, residual tolerance
     1e-7, ft = 6, Gf = 10, E = 1.  Wall time of nbg_fem_damage (device
-    assembly with damage, boundary conditions, residual, nbots-order Jacobi
-    PCG, strain and damage, host log) against the oracle's one-thread
+    assembly with damage, boundary conditions, residual, Jacobi-PCG with
+    nbots' iteration and stop test on the block layout (the drop-in's inner
+    solver), strain and damage, host log) against the oracle's one-thread
     restatement of nbots' loop on the same problem; and the same device loop
-    with the fast FP64 block CG as its inner solver."""
+    with nbots' operation order on the CSR and with the fast FP64 block CG
+    as its inner solver."""
     import tempfile
     from nbots_gb300.fem import FemSystem
     out = {}
     args_ = (6.0, 10.0, 4, 40, 6, 1e-7)
-    for method in (L.METHOD_NBOTS, L.METHOD_FP64):  # warm: modules, first launches
+    for method in (L.METHOD_NBOTS_FAST, L.METHOD_NBOTS, L.METHOD_FP64):  # warm the modules
         s = FemSystem(W.cantilever_q4(16, 8, point_load=0.0, top_traction=0.35))
         s.damage(*args_, method=method)
         s.close()
     for nx, ny, cpu in ((128, 64, with_cpu), (512, 256, False)):
         p = W.cantilever_q4(nx, ny, point_load=0.0, top_traction=0.35)
         row = {"workload": f"Q4 cantilever {nx}x{ny}, {p.n_dof} dof, top traction 0.35"}
-        for method, key in ((L.METHOD_NBOTS, "nbots_cg"), (L.METHOD_FP64, "fast_fp64_cg")):
+        for method, key in ((L.METHOD_NBOTS_FAST, "nbots_iteration_block_cg"),
+                            (L.METHOD_NBOTS, "nbots_order_cg"), (L.METHOD_FP64, "fast_fp64_cg")):
             s = FemSystem(p)
             with tempfile.TemporaryDirectory() as td:
                 logf = os.path.join(td, "dmg.log")
@@ -290,7 +316,7 @@ def bench_damage(L, W, with_cpu):
                    "cg_solves": info.cg_solves, "cg_iterations": info.cg_iterations,
                    "gs_fallbacks": info.gs_fallbacks,
                    "step_iterations": _damage_step_iters(log)}
-            if method == L.METHOD_NBOTS:
+            if method == L.METHOD_NBOTS_FAST:
                 row.update(res)  # the drop-in's inner solver: the row's headline
             else:
                 row[key] = res
@@ -761,6 +787,7 @@ def run_gpu(args):
 
     clk = Clocks(local)
     t_mixed, r_mixed = timed(mixed, args.steps, args.warmup, clk)
+    mixed_form = lib.nbg_cg_mixed_last_form()
     u_mixed = u.clone()
     t_fp64, r_fp64 = timed(fp64, max(1, min(args.steps, 3)), 1)
     u_fp64 = u.clone()
@@ -877,7 +904,17 @@ def run_gpu(args):
     # column per block), u and b, writes u.
     it = r_mixed.niter
     t_med = float(np.median(t_mixed))
-    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 24 * N
+    form = mixed_form
+    if form == 2:
+        # ghost-node form: 26 B per block (16-bit local column), and per dof r
+        # published (4 B), x in and out (16 B), 1/Aii in L2 and L3 (8 B), plus
+        # r and 1/Aii of every block's ghosts (8 B per ghost dof)
+        ghost_dofs = 2 * ghost_count(s.get(L.FEM_ROW_PTR), s.get(L.FEM_COL_IDX), A.n_slices,
+                                     mixed_blocks(A.n_slices, dev))
+        bytes_iter = 26 * nblk + 4 * (A.n_slices + 1) + 28 * N + 8 * ghost_dofs
+    else:
+        ghost_dofs = 0
+        bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 24 * N
     upd_bytes = (r_mixed.n_updates + 1) * (36 * nblk + 4 * (A.n_slices + 1) + 24 * N)
     achieved = (bytes_iter * it + upd_bytes) / t_med / 1e9
     # fast FP64 kernel (vectors in global memory): 36 B per block, and per dof
@@ -986,8 +1023,10 @@ def run_gpu(args):
             "spmv": spmv,
             "roofline": {"bound": "hbm", "achieved": achieved, "peak": hbm, "unit": "GB/s",
                          "frac": achieved / hbm, "peak_kind": peak_kind,
-                         "traffic": traffic, "kernel": "k_cg_mixed",
-                         "bytes_per_iter": bytes_iter,
+                         "traffic": traffic,
+                         "kernel": "k_cg_mixed_ghost" if form == 2 else "k_cg_mixed",
+                         "form": ["global rows", "resident rows", "ghost nodes"][form],
+                         "ghost_dofs": ghost_dofs, "bytes_per_iter": bytes_iter,
                          "note": "traffic is DRAM bytes per iteration from ncu; below "
                                  "bytes_per_iter because part of the matrix stays in L2 "
                                  "(evict_last) between iterations"},

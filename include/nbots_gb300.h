@@ -315,6 +315,11 @@ int nbg_spmv_bsr_mixed(const nbg_bsr_t *A, const float *ph, const float *pl, flo
  * same bit for bit.  ws NULL allocates the larger size. */
 size_t nbg_cg_mixed_workspace_bytes(uint32_t N);
 size_t nbg_cg_mixed_layout_workspace_bytes(const nbg_bsr_t *A);
+/* The form the calling thread's last nbg_cg_mixed launch took. */
+#define NBG_MIXED_GLOBAL_ROWS 0   /* own rows and p in global memory */
+#define NBG_MIXED_RESIDENT_ROWS 1 /* own rows in shared memory, p gathered from global */
+#define NBG_MIXED_GHOST 2         /* own rows and ghosts in shared memory */
+int nbg_cg_mixed_last_form(void);
 int nbg_cg_mixed(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_iter,
                  double tol, double delta, unsigned flags, nbg_mixed_result_t *result,
                  void *ws, size_t ws_bytes, void *stream);

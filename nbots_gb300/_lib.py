@@ -123,6 +123,7 @@ SIGS = {
     "nbg_spmv_bsr_mixed": ([C.POINTER(Bsr), vp, vp, vp, vp, vp], i32),
     "nbg_cg_mixed_workspace_bytes": ([u32], sz),
     "nbg_cg_mixed_layout_workspace_bytes": ([C.POINTER(Bsr)], sz),
+    "nbg_cg_mixed_last_form": ([], i32),
     "nbg_cg_mixed": ([C.POINTER(Bsr), vp, vp, u32, f64, f64, C.c_uint,
                       C.POINTER(MixedResult), vp, sz, vp], i32),
     "nbg_fem_block_layout": ([vp, C.POINTER(Bsr)], i32),

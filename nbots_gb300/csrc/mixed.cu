@@ -1089,6 +1089,12 @@ extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const flo
 
 extern "C" size_t nbg_cg_mixed_workspace_bytes(uint32_t N) { return mixed_bytes(N); }
 
+namespace {
+thread_local int g_mixed_form = 0;  // form of this thread's last nbg_cg_mixed launch
+}  // namespace
+
+extern "C" int nbg_cg_mixed_last_form(void) { return g_mixed_form; }
+
 extern "C" size_t nbg_cg_mixed_layout_workspace_bytes(const nbg_bsr_t* A) {
     return A ? mixed_bytes(A->N) + ghost_plan_bytes(*A) : 0;
 }
@@ -1246,6 +1252,8 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     g.g_size = G;
     g.pstride = kMaxBlocks;
     if (ghost) a.keep_pm = keep_permille(*A, 26.0);
+    g_mixed_form = ghost ? NBG_MIXED_GHOST : a.resident ? NBG_MIXED_RESIDENT_ROWS
+                                                       : NBG_MIXED_GLOBAL_ROWS;
     if (e == cudaSuccess && rc == NBG_OK) {
         void* args[] = {&a, &g, &gh};
         e = cudaLaunchCooperativeKernel(fn, dim3(G), dim3(kMixThreads),
