@@ -116,7 +116,8 @@ void nb_sparse_fill_permutation(const nb_sparse_t *A, nb_sparse_t *Ar, const uin
  * functions above mark it changed, so the next GPU call re-sends the values
  * (the pattern never changes), and nb_sparse_destroy frees the copy.  Code
  * that writes rows_values directly calls nbg_dropin_sparse_touch(A) before
- * the next GPU call.  NBG_DROPIN_CACHE_MB (default 16384) bounds the device
+ * the next GPU call, and so does code that points a row at other memory.
+ * NBG_DROPIN_CACHE_MB (default 16384) bounds the device
  * memory of all copies (least recently used dropped first; 0: no copies).
  * Matrices nbots allocated itself are sent whole on every call. */
 void nbg_dropin_sparse_touch(const nb_sparse_t *A);

@@ -605,6 +605,9 @@ __global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
 //
 // The plan (ghost lists, local columns) depends on the launch's block
 // partition and is rebuilt by a short kernel at the start of every solve.
+#ifndef NBG_MIXED_SO_SMEM
+#define NBG_MIXED_SO_SMEM 1  // the block's slice offsets in shared memory
+#endif
 constexpr uint32_t kGhostMax = 16384;   // ghosts per block
 constexpr uint32_t kGhostKeys = 32768;  // outside-column references per block the plan sorts
 
@@ -734,13 +737,14 @@ __global__ void __launch_bounds__(1024, 1) k_ghost_plan(nbg_bsr_t A, uint16_t* l
 // memory as float4 {hi of both dofs, lo of both dofs}; the same products and
 // sums in the same order.
 __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t* __restrict__ lcol,
-                                                const float4* P, uint32_t s, uint32_t r,
-                                                uint32_t par, bool live, uint64_t pol, FF& y0,
-                                                FF& y1) {
+                                                const float4* P, const uint32_t* so,
+                                                uint32_t s, uint32_t r, uint32_t par, bool live,
+                                                uint64_t pol, FF& y0, FF& y1) {
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
     FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
-    const uint32_t k0 = a.A.slice_off[s] + par, k1 = live ? a.A.slice_off[s + 1] : 0;
+    // so: this block's slice offsets, so[0] that of its first slice
+    const uint32_t k0 = so[s] + par, k1 = live ? so[s + 1] : 0;
 #pragma unroll(kUnroll)
     for (uint32_t k = k0; k < k1; k += 2) {
         const size_t e = (size_t)k * 32 + r;
@@ -820,6 +824,9 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
     float2* const WH = R + gh.scap;
     float2* const WL = WH + gh.scap;
     uint32_t* const GID = reinterpret_cast<uint32_t*>(WL + gh.scap);
+    // slice offsets of this block, indexed by s - s0
+    uint32_t* const SO = NBG_MIXED_SO_SMEM ? GID + gh.gcap
+                                           : const_cast<uint32_t*>(a.A.slice_off) + s0;
     float2* __restrict__ gr = reinterpret_cast<float2*>(a.r);
     float2* __restrict__ xh = reinterpret_cast<float2*>(a.xh);
     float2* __restrict__ xl = reinterpret_cast<float2*>(a.xl);
@@ -835,6 +842,8 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         sc.converged = 0;
     }
     for (uint32_t j = tid; j < ng; j += kThreads) GID[j] = gh.ids[(size_t)rank * kGhostMax + j];
+    if (NBG_MIXED_SO_SMEM)
+        for (uint32_t j = tid; j <= s1 - s0; j += kThreads) SO[j] = a.A.slice_off[s0 + j];
     {   // init: x = 0, r = b - A u (FP64), own p = z, r published
         for (uint32_t s = s0 + warp; s < s1; s += nw) {
             const uint32_t i = s * 32 + lane;
@@ -881,7 +890,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
                 if (s * 32 + ((h & 1) << 4) >= Nn) continue;
                 FF y0, y1;
                 const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
-                spmv_half_local(a, gh.lcol, P, s, r, par, i < Nn, pol, y0, y1);
+                spmv_half_local(a, gh.lcol, P, SO, s - s0, r, par, i < Nn, pol, y0, y1);
                 if (par || i >= Nn) continue;
                 WH[li] = make_float2(y0.hi, y1.hi);
                 WL[li] = make_float2(y0.lo, y1.lo);
@@ -1140,7 +1149,8 @@ int ghost_setup(const nbg_bsr_t& A, unsigned G, char* plan, cudaStream_t s, Ghos
         pcap = std::max(pcap, 32 * (s1 - s0) + cnt[b]);
         gcap = std::max(gcap, cnt[b]);
     }
-    const size_t bytes = 16 * (size_t)pcap + 24 * (size_t)scap + 4 * (size_t)gcap;
+    const size_t bytes = 16 * (size_t)pcap + 24 * (size_t)scap + 4 * (size_t)gcap +
+                         (NBG_MIXED_SO_SMEM ? 4 * ((size_t)scap / 32 + 1) : 0);
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, (const void*)k_cg_mixed_ghost) != cudaSuccess ||
         bytes + fa.sharedSizeBytes > (size_t)optin)

@@ -596,7 +596,10 @@ static slab_t *lock_device(const nb_sparse_t *A, int send_values, int *rc)
 	if (!s || cache_limit() == 0)
 		return NULL;
 	pthread_mutex_lock(&s->lock);
-	if (!in_slabs(s)) {
+	/* the layout is checked whenever the copy is built or re-sent; a clean
+	 * copy is used as it is (rows moved by direct writes are announced with
+	 * nbg_dropin_sparse_touch, which marks the matrix changed) */
+	if ((!s->dev || s->dirty) && !in_slabs(s)) {
 		drop_device(s);
 		pthread_mutex_unlock(&s->lock);
 		return NULL;
