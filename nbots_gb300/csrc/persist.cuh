@@ -175,20 +175,34 @@ __device__ __forceinline__ void group_publish_ff(FF (&v)[NV], float2* scratch, f
 // Sum over the group's blocks of NV float-float partials, in block order, by
 // warp 0 with error-free FP32 arithmetic; the result (as FP64) is valid in
 // thread 0 only (no block synchronisation).
+// Lane l adds the partials of blocks l, l + 32, ... in that order; the
+// loads of kReduceBatch of them go out before the first add (one L2 round
+// trip per batch instead of one per partial: 152 blocks, 5 per lane, is one
+// batch).
+constexpr int kReduceBatch = 5;
+
 template <int NV>
 __device__ __forceinline__ void group_reduce0_ff(const float2* part, uint32_t G,
                                                  double (&out)[NV]) {
     if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
+        const uint32_t lane = threadIdx.x;
         FF v[NV];
 #pragma unroll
-        for (int k = 0; k < NV; k++) {
-            v[k] = FF{0.f, 0.f};
-#pragma unroll 8
-            for (unsigned b = lane; b < G; b += 32) {
-                const float2 t = part[b * NV + k];
-                v[k] = ff_add(v[k], FF{t.x, t.y});
+        for (int k = 0; k < NV; k++) v[k] = FF{0.f, 0.f};
+        for (uint32_t base = 0; base < G; base += 32 * kReduceBatch) {
+            float2 t[kReduceBatch][NV];
+#pragma unroll
+            for (int j = 0; j < kReduceBatch; j++) {
+                const uint32_t b = base + 32 * j + lane;
+#pragma unroll
+                for (int k = 0; k < NV; k++)
+                    t[j][k] = b < G ? part[b * NV + k] : make_float2(0.f, 0.f);
             }
+#pragma unroll
+            for (int j = 0; j < kReduceBatch; j++)
+                if (base + 32 * j + lane < G)
+#pragma unroll
+                    for (int k = 0; k < NV; k++) v[k] = ff_add(v[k], FF{t[j][k].x, t[j][k].y});
         }
         ff_warp_sum<NV>(v);
 #pragma unroll
@@ -227,15 +241,29 @@ __device__ __forceinline__ void block_sum_f64(const double (&v)[NV], double* buf
 template <int NV>
 __device__ __forceinline__ void group_reduce0(const double* part, uint32_t G, double (&out)[NV]) {
     if (threadIdx.x < 32) {
-        const int lane = threadIdx.x;
+        const uint32_t lane = threadIdx.x;
+        double s[NV];
+#pragma unroll
+        for (int k = 0; k < NV; k++) s[k] = 0.0;
+        for (uint32_t base = 0; base < G; base += 32 * kReduceBatch) {
+            double t[kReduceBatch][NV];
+#pragma unroll
+            for (int j = 0; j < kReduceBatch; j++) {
+                const uint32_t b = base + 32 * j + lane;
+#pragma unroll
+                for (int k = 0; k < NV; k++) t[j][k] = b < G ? part[b * NV + k] : 0.0;
+            }
+#pragma unroll
+            for (int j = 0; j < kReduceBatch; j++)
+                if (base + 32 * j + lane < G)
+#pragma unroll
+                    for (int k = 0; k < NV; k++) s[k] += t[j][k];
+        }
 #pragma unroll
         for (int k = 0; k < NV; k++) {
-            double s = 0.0;
-#pragma unroll 8
-            for (unsigned b = lane; b < G; b += 32) s += part[b * NV + k];
 #pragma unroll
-            for (int o = 16; o > 0; o >>= 1) s += __shfl_down_sync(0xffffffffu, s, o);
-            out[k] = s;
+            for (int o = 16; o > 0; o >>= 1) s[k] += __shfl_down_sync(0xffffffffu, s[k], o);
+            out[k] = s[k];
         }
     }
 }
