@@ -279,6 +279,8 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
 // memory as FP32 pairs and flags.
 template <bool kRes, int kThreads>
 __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, unsigned char* smem) {
+    // batched launches give each system at most a few dozen blocks
+    constexpr int kRB = kThreads == kMixThreads ? kReduceBatch : 1;
     __shared__ double red[3 * 32];
     float2* const ffred = reinterpret_cast<float2*>(red);
     __shared__ float s_alpha[2], s_beta[2];
@@ -369,7 +371,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
         if (sync()) goto done;
         {
             double pwd[1];
-            group_reduce0_ff<1>(reinterpret_cast<const float2*>(part0), G, pwd);
+            group_reduce0_ff<1, kRB>(reinterpret_cast<const float2*>(part0), G, pwd);
             if (threadIdx.x == 0) {
                 const FF al = ff_from_double(sc.rz / pwd[0]);
                 s_alpha[0] = al.hi;
@@ -408,7 +410,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
         if (sync()) goto done;
         {
             double t2[2];
-            group_reduce0_ff<2>(reinterpret_cast<const float2*>(part1), G, t2);
+            group_reduce0_ff<2, kRB>(reinterpret_cast<const float2*>(part1), G, t2);
             if (threadIdx.x == 0) {
                 const double rz_new = t2[0], rr = t2[1];
                 if (rr > sc.rmax2) sc.rmax2 = rr;

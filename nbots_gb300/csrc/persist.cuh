@@ -178,10 +178,10 @@ __device__ __forceinline__ void group_publish_ff(FF (&v)[NV], float2* scratch, f
 // Lane l adds the partials of blocks l, l + 32, ... in that order; the
 // loads of kReduceBatch of them go out before the first add (one L2 round
 // trip per batch instead of one per partial: 152 blocks, 5 per lane, is one
-// batch).
+// batch).  Launches whose groups have at most 32 blocks pass 1.
 constexpr int kReduceBatch = 5;
 
-template <int NV>
+template <int NV, int kReduceBatch = kReduceBatch>
 __device__ __forceinline__ void group_reduce0_ff(const float2* part, uint32_t G,
                                                  double (&out)[NV]) {
     if (threadIdx.x < 32) {
