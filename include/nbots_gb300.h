@@ -243,11 +243,6 @@ typedef struct {
      * original node order whatever the order. */
     const uint32_t *perm;
     const uint32_t *iperm;
-    /* Optional (device, NULL = none): blocks of each slice row (the rest of
-     * its slice width is padding, zero values pointing at the row itself).
-     * With it the SpMVs and solvers skip the padding, which changes no
-     * result bit; unstructured meshes pad their slices by up to half. */
-    const uint16_t *rlen;
 } nbg_bsr_t;
 
 /* Device: a SELL-C-sigma node order of a node-blocked CSR (row_ptr on the

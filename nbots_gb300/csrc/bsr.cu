@@ -27,8 +27,7 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
                            const uint32_t* __restrict__ perm, const uint32_t* __restrict__ iperm,
                            uint32_t* __restrict__ bcol, double* __restrict__ b64,
                            float* __restrict__ b32, uint16_t* __restrict__ blo,
-                           double* __restrict__ dinv64, float* __restrict__ dinv32,
-                           uint16_t* __restrict__ rlen) {
+                           double* __restrict__ dinv64, float* __restrict__ dinv32) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Nn) return;
     const uint32_t s = i >> 5, lane = i & 31;
@@ -36,7 +35,6 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
     const uint32_t width = slice_off[s + 1] - slice_off[s];
     const uint32_t r0 = rp[2 * v], r1 = rp[2 * v + 1];
     const uint32_t nb = (r1 - r0) / 2;
-    if (rlen) rlen[i] = (uint16_t)nb;  // nb <= width, which the plan keeps below 65536
     double d0 = 0.0, d1 = 0.0;
     for (uint32_t k = 0; k < width; k++) {
         const size_t e = ((size_t)slice_off[s] + k) * 32 + lane;
@@ -86,7 +84,6 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
 }
 
 __global__ void __launch_bounds__(256) k_spmv_bsr_f64(uint32_t Nn, const uint32_t* __restrict__ so,
-                                                      const uint16_t* __restrict__ rlen,
                                                       const uint32_t* __restrict__ bcol,
                                                       const double* __restrict__ b64,
                                                       const double* __restrict__ x,
@@ -94,7 +91,7 @@ __global__ void __launch_bounds__(256) k_spmv_bsr_f64(uint32_t Nn, const uint32_
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Nn) return;
     const uint32_t s = i >> 5, lane = i & 31;
-    const uint32_t k0 = so[s], k1 = rlen ? k0 + rlen[i] : so[s + 1];  // padding skipped
+    const uint32_t k0 = so[s], k1 = so[s + 1];
     const double2* __restrict__ xv = reinterpret_cast<const double2*>(x);
     const double2* __restrict__ bv = reinterpret_cast<const double2*>(b64);
     const uint64_t pol = l2_policy(false);  // the matrix streams through L2 once
@@ -113,7 +110,6 @@ __global__ void __launch_bounds__(256) k_spmv_bsr_f64(uint32_t Nn, const uint32_
 }
 
 __global__ void __launch_bounds__(256) k_spmv_bsr_f32(uint32_t Nn, const uint32_t* __restrict__ so,
-                                                      const uint16_t* __restrict__ rlen,
                                                       const uint32_t* __restrict__ bcol,
                                                       const float* __restrict__ b32,
                                                       const float* __restrict__ x,
@@ -121,7 +117,7 @@ __global__ void __launch_bounds__(256) k_spmv_bsr_f32(uint32_t Nn, const uint32_
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Nn) return;
     const uint32_t s = i >> 5, lane = i & 31;
-    const uint32_t k0 = so[s], k1 = rlen ? k0 + rlen[i] : so[s + 1];  // padding skipped
+    const uint32_t k0 = so[s], k1 = so[s + 1];
     const float2* __restrict__ xv = reinterpret_cast<const float2*>(x);
     const float4* __restrict__ bv = reinterpret_cast<const float4*>(b32);
     const uint64_t pol = l2_policy(false);  // the matrix streams through L2 once
@@ -158,7 +154,6 @@ extern "C" int nbg_bsr_plan(uint32_t N, const uint32_t* row_ptr, const uint32_t*
                     return NBG_ERR_PATTERN;
             }
             if ((b - a) / 2 > w) w = (b - a) / 2;
-            if (w > 65535u) return NBG_ERR_PATTERN;  // row block counts are 16-bit
         }
         slice_off[s + 1] = slice_off[s] + w;
     }
@@ -172,7 +167,7 @@ extern "C" int nbg_bsr_fill(const nbg_bsr_t* A, const uint32_t* row_ptr, const u
     k_bsr_fill<<<(A->Nn + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
         A->Nn, row_ptr, col_idx, val, A->slice_off, A->perm, A->iperm, (uint32_t*)A->bcol,
         (double*)A->b64, (float*)A->b32, (uint16_t*)A->blo, (double*)A->dinv64,
-        (float*)A->dinv32, (uint16_t*)A->rlen);
+        (float*)A->dinv32);
     NBG_CHECK(cudaGetLastError());
     return NBG_OK;
 }
@@ -205,7 +200,7 @@ extern "C" int nbg_spmv_bsr_f64(const nbg_bsr_t* A, const double* x, double* y, 
     if (!A->b64) return NBG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     return spmv_perm(A, x, y, s, [&](const double* xx, double* yy) {
-        k_spmv_bsr_f64<<<(A->Nn + 255) / 256, 256, 0, s>>>(A->Nn, A->slice_off, A->rlen, A->bcol, A->b64,
+        k_spmv_bsr_f64<<<(A->Nn + 255) / 256, 256, 0, s>>>(A->Nn, A->slice_off, A->bcol, A->b64,
                                                             xx, yy);
     });
 }
@@ -215,7 +210,7 @@ extern "C" int nbg_spmv_bsr_f32(const nbg_bsr_t* A, const float* x, float* y, vo
     if (!A->b32) return NBG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     return spmv_perm(A, x, y, s, [&](const float* xx, float* yy) {
-        k_spmv_bsr_f32<<<(A->Nn + 255) / 256, 256, 0, s>>>(A->Nn, A->slice_off, A->rlen, A->bcol, A->b32,
+        k_spmv_bsr_f32<<<(A->Nn + 255) / 256, 256, 0, s>>>(A->Nn, A->slice_off, A->bcol, A->b32,
                                                             xx, yy);
     });
 }

@@ -169,9 +169,7 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
     // rows past Nn in the last slice hold no entries: such lanes only
     // take part in the exchange
-    // the row's own blocks when their count is known, else the slice width
-    const uint32_t kb = a.A.slice_off[s], k0 = kb + par;
-    const uint32_t k1 = !live ? 0 : a.A.rlen ? kb + a.A.rlen[(size_t)s * 32 + r] : a.A.slice_off[s + 1];
+    const uint32_t k0 = a.A.slice_off[s] + par, k1 = live ? a.A.slice_off[s + 1] : 0;
 #pragma unroll(kUnroll)
     for (uint32_t k = k0; k < k1; k += 2) {
         const size_t e = (size_t)k * 32 + r;
@@ -743,13 +741,12 @@ __global__ void __launch_bounds__(1024, 1) k_ghost_plan(nbg_bsr_t A, uint16_t* l
 __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t* __restrict__ lcol,
                                                 const float4* P, const uint32_t* so,
                                                 uint32_t s, uint32_t r, uint32_t par, bool live,
-                                                uint32_t grow, uint64_t pol, FF& y0, FF& y1) {
+                                                uint64_t pol, FF& y0, FF& y1) {
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
     FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
     // so: this block's slice offsets, so[0] that of its first slice
-    const uint32_t k0 = so[s] + par;
-    const uint32_t k1 = !live ? 0 : a.A.rlen ? so[s] + a.A.rlen[grow] : so[s + 1];
+    const uint32_t k0 = so[s] + par, k1 = live ? so[s + 1] : 0;
 #pragma unroll(kUnroll)
     for (uint32_t k = k0; k < k1; k += 2) {
         const size_t e = (size_t)k * 32 + r;
@@ -895,7 +892,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
                 if (s * 32 + ((h & 1) << 4) >= Nn) continue;
                 FF y0, y1;
                 const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
-                spmv_half_local(a, gh.lcol, P, SO, s - s0, r, par, i < Nn, i, pol, y0, y1);
+                spmv_half_local(a, gh.lcol, P, SO, s - s0, r, par, i < Nn, pol, y0, y1);
                 if (par || i >= Nn) continue;
                 WH[li] = make_float2(y0.hi, y1.hi);
                 WL[li] = make_float2(y0.lo, y1.lo);

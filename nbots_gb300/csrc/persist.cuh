@@ -276,8 +276,7 @@ __device__ __forceinline__ double2 spmv_row_f64(const nbg_bsr_t& A, uint32_t s, 
     // evict_first keeps the vectors there (1M dof: 64.3 -> 62.8 us/iteration)
     const uint64_t pol = l2_policy(false);
     double y0 = 0.0, y1 = 0.0;
-    const uint32_t k0 = A.slice_off[s];
-    const uint32_t k1 = A.rlen ? k0 + A.rlen[s * 32 + lane] : A.slice_off[s + 1];
+    const uint32_t k0 = A.slice_off[s], k1 = A.slice_off[s + 1];
 #pragma unroll 3
     for (uint32_t k = k0; k < k1; k++) {
         const size_t e = (size_t)k * 32 + lane;

@@ -22,7 +22,7 @@ struct nbg_solver {
 	uint32_t *rp, *ci, *slice_off, *bcol;
 	double *val, *b, *x, *b64, *dinv64;
 	float *b32, *dinv32;
-	uint16_t *blo, *rlen;
+	uint16_t *blo;
 	void *ws;
 	size_t ws_bytes;
 	nbg_bsr_t bsr;
@@ -31,7 +31,7 @@ struct nbg_solver {
 static void release(nbg_solver_t *s)
 {
 	void *p[] = {s->rp, s->ci, s->slice_off, s->bcol, s->val, s->b, s->x, s->b64,
-		     s->dinv64, s->b32, s->dinv32, s->blo, s->rlen, s->ws};
+		     s->dinv64, s->b32, s->dinv32, s->blo, s->ws};
 	for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++)
 		nbg_dev_free(p[i]);
 	void *stream = s->stream;
@@ -93,7 +93,6 @@ int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->blo, 8 * ent);
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->dinv64, 8 * (size_t)N);
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->dinv32, 4 * (size_t)N);
-			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->rlen, 2 * (size_t)(N / 2));
 			if (r2 == NBG_OK) r2 = nbg_stream_sync(s->stream);
 			free(so);
 			so = NULL;
@@ -109,7 +108,6 @@ int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
 			s->bsr.blo = s->blo;
 			s->bsr.dinv64 = s->dinv64;
 			s->bsr.dinv32 = s->dinv32;
-			s->bsr.rlen = s->rlen;
 		}
 		free(so);
 		s->have_pattern = 1;
@@ -228,7 +226,7 @@ size_t nbg_solver_device_bytes(const nbg_solver_t *s)
 	size_t b = 4 * ((size_t)s->N + 1) + 12 * (size_t)s->nnz + 16 * (size_t)s->N + s->ws_bytes;
 	if (s->bsr_ok)
 		b += 4 * ((size_t)s->bsr.n_slices + 1) + 60 * (size_t)s->bsr.n_entries +
-		     13 * (size_t)s->N;
+		     12 * (size_t)s->N;
 	return b;
 }
 

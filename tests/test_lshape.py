@@ -58,11 +58,12 @@ def test_lshape_assembly_and_solvers_on_gpu():
     assert np.array_equal(s.get(L.FEM_F).view(np.uint64), r["F_bc"].view(np.uint64))
     rp, ci, K, F = r["row_ptr"], r["col_idx"], r["K_bc"], r["F_bc"]
     tight, *_ = O.cg_jacobi(rp, ci, K, F, max_iter=40 * F.shape[0], tol=1e-13 * np.linalg.norm(F))
-    # Both fast solvers judge convergence on the true FP64 residual (the FP64
-    # CG confirms its recurrence's verdict on b - A u), so both must meet the
-    # tolerance on the oracle's SpMV.  They run on a layout in SELL-C-sigma
-    # node order and in mesh order (the default); the mesh order stores
-    # about 40 % more entries here
+    # The fast FP64 solver stops on its recursively updated residual, as
+    # nbots does; on this mesh (re-entrant corner) the true residual of FP64
+    # CG levels off near 1e-10, so it is checked at 1e-10 with a factor 2 for
+    # that gap.  The mixed solver judges the recomputed FP64 residual itself.
+    # the solvers on a layout in SELL-C-sigma node order and in mesh order
+    # (the default); the mesh order stores about 40 % more entries here
     m = FemSystem(p)
     assert m.assemble() == 0
     m.apply_bcs()
@@ -80,58 +81,4 @@ def test_lshape_assembly_and_solvers_on_gpu():
             assert rr <= slack * tol, (solve.__name__, rr)
             assert np.linalg.norm(u - tight) / np.linalg.norm(tight) < uerr
     m.close()
-    s.close()
-
-
-@pytest.mark.gpu
-def test_padding_skip_changes_no_bit():
-    """The block layout's slices are as wide as their longest row; on this
-    unstructured mesh that pads them by about 40 %.  With the row block
-    counts (nbg_bsr_t.rlen) the SpMVs and the solvers stop each row at its
-    own length; the padding holds zero values, so the products, the
-    iterates and the solutions are the same bit for bit as without the
-    counts."""
-    import ctypes as C
-    from nbots_gb300 import _lib as L
-    from nbots_gb300.device import DeviceArray
-    from nbots_gb300.fem import FemSystem
-    lib = L.lib()
-    p = lshape(20000)
-    s = FemSystem(p)
-    assert s.assemble() == 0
-    s.apply_bcs()
-    A = s.block_layout()
-    assert A.rlen and A.n_entries > 1.2 * (s.nnz // 4)
-    B = L.Bsr.from_buffer_copy(A)
-    B.rlen = None
-    N, F = s.N, s.dptr(L.FEM_F)
-    x = np.random.default_rng(5).standard_normal(N)
-    dx, dy = DeviceArray(x), DeviceArray(shape=(N,), dtype=np.float64)
-    x32 = DeviceArray(x.astype(np.float32))
-    y32 = DeviceArray(shape=(N,), dtype=np.float32)
-    out = []
-    for lay in (A, B):
-        L.check(lib.nbg_spmv_bsr_f64(C.byref(lay), dx.ptr, dy.ptr, None), "spmv64")
-        L.check(lib.nbg_spmv_bsr_f32(C.byref(lay), x32.ptr, y32.ptr, None), "spmv32")
-        res = [dy.numpy().view(np.uint64), y32.numpy().view(np.uint32)]
-        for flags in (L.CG_JACOBI | L.CG_RELATIVE, L.CG_JACOBI | L.CG_NBOTS_STOP):
-            u = DeviceArray(np.zeros(N))
-            r = L.CgResult()
-            rc = lib.nbg_cg_bsr_f64(C.byref(lay), F, u.ptr, 4 * N,
-                                    1e-10 if flags & L.CG_RELATIVE else 1e-9, flags,
-                                    C.byref(r), None, 0, None)
-            assert rc == 0
-            res += [r.niter, u.numpy().view(np.uint64)]
-        for ws in (lib.nbg_cg_mixed_workspace_bytes(N),
-                   lib.nbg_cg_mixed_layout_workspace_bytes(C.byref(lay))):
-            u = DeviceArray(np.zeros(N))
-            w = DeviceArray(shape=(ws,), dtype=np.uint8)
-            r = L.MixedResult()
-            rc = lib.nbg_cg_mixed(C.byref(lay), F, u.ptr, 8 * N, 1e-10, 0.1,
-                                  L.CG_JACOBI | L.CG_RELATIVE, C.byref(r), w.ptr, ws, None)
-            assert rc == 0
-            res += [r.niter, u.numpy().view(np.uint64)]
-        out.append(res)
-    for a, b in zip(*out):
-        assert np.array_equal(a, b)
     s.close()
