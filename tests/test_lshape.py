@@ -58,12 +58,11 @@ def test_lshape_assembly_and_solvers_on_gpu():
     assert np.array_equal(s.get(L.FEM_F).view(np.uint64), r["F_bc"].view(np.uint64))
     rp, ci, K, F = r["row_ptr"], r["col_idx"], r["K_bc"], r["F_bc"]
     tight, *_ = O.cg_jacobi(rp, ci, K, F, max_iter=40 * F.shape[0], tol=1e-13 * np.linalg.norm(F))
-    # The fast FP64 solver stops on its recursively updated residual, as
-    # nbots does; on this mesh (re-entrant corner) the true residual of FP64
-    # CG levels off near 1e-10, so it is checked at 1e-10 with a factor 2 for
-    # that gap.  The mixed solver judges the recomputed FP64 residual itself.
-    # the solvers on a layout in SELL-C-sigma node order and in mesh order
-    # (the default); the mesh order stores about 40 % more entries here
+    # Both fast solvers judge convergence on the true FP64 residual (the FP64
+    # CG confirms its recurrence's verdict on b - A u), so both must meet the
+    # tolerance on the oracle's SpMV.  They run on a layout in SELL-C-sigma
+    # node order and in mesh order (the default); the mesh order stores
+    # about 40 % more entries here
     m = FemSystem(p)
     assert m.assemble() == 0
     m.apply_bcs()
