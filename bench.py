@@ -1042,7 +1042,9 @@ def run_gpu(args):
             "c5_batch": c5,
             "damage": dmg,
             "cpu_baseline": cpu,
-            "gpu_launches": args.steps,
+            # per timed step: the ghost plan and the solver (ghost form), or
+            # the solver alone
+            "gpu_launches": args.steps * (2 if form == 2 else 1),
             "dof_iters_per_s": N * it / t_all,
             "clocks": clk.summary(),
         }
