@@ -111,3 +111,47 @@ def test_clone_and_destroy_with_replaced_rows():
     B.contents.rows_index[3] = C.cast(newi, C.POINTER(C.c_uint32))
     G.nb_sparse_destroy(B)
     G.nb_sparse_destroy(A)
+
+
+def test_registry_under_threads():
+    """Matrices created, written and destroyed from several threads at once
+    (the registry of slab-backed matrices, its epoch and the per-thread memo
+    of the last lookup that every nb_sparse_add consults): every matrix ends
+    with the sums its own thread added, and destroy frees everything without
+    error.  ctypes releases the interpreter lock around each C call, so the
+    threads do run the C code concurrently."""
+    import threading
+    from nbots_gb300 import workloads as W
+    from nbots_gb300.dropin import csr_of, libs, nodal_graph
+    G, _ = libs()
+    p = W.cantilever_q4(8, 4)
+    g, keep = nodal_graph(p)
+    fl = O.Flat(p)
+    rp, ci = O.pattern(fl)
+    errors = []
+
+    def work(seed):
+        try:
+            rng = np.random.default_rng(seed)
+            for _ in range(30):
+                mats = [G.nb_sparse_create(C.byref(g), None, 2) for _ in range(3)]
+                want = [np.zeros(ci.shape[0]) for _ in mats]
+                for _ in range(200):
+                    m = int(rng.integers(len(mats)))
+                    k = int(rng.integers(ci.shape[0]))
+                    i = int(np.searchsorted(rp, k, side="right") - 1)
+                    G.nb_sparse_add(mats[m], i, int(ci[k]), 1.0)
+                    want[m][k] += 1.0
+                for A, w in zip(mats, want):
+                    if not np.array_equal(csr_of(A)[2], w):
+                        errors.append("values")
+                    G.nb_sparse_destroy(A)
+        except Exception as e:  # reported below
+            errors.append(repr(e))
+    ts = [threading.Thread(target=work, args=(s,)) for s in range(4)]
+    for t in ts:
+        t.start()
+    for t in ts:
+        t.join()
+    assert not errors, errors[:3]
+    assert G.nbg_dropin_error() == 0
