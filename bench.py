@@ -638,9 +638,9 @@ def bench_c3(args, with_cpu):
     m.close()
     # own rows do not fit in shared memory at this size, so besides the p
     # exchange and 1/Aii (24 B/dof) they move through global memory: per node
-    # L1 w out, p in (16 + 16 B), L2 p, w, x, r in (16 + 16 + 16 + 8 B) and
-    # x, r out (16 + 8 B), L3 r, p in (8 + 16 B): 136 B
-    bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 24 * N + 136 * (N // 2)
+    # L1 w out, p in (16 + 16 B), L2 p, w, x, r in (16 + 16 + 16 + 16 B) and
+    # x, r out (16 + 16 B), L3 r, p in (16 + 16 B): 160 B
+    bytes_iter = 32 * nblk + 4 * (A.n_slices + 1) + 24 * N + 160 * (N // 2)
     hbm, peak_kind = peaks()
     cpu = None
     if with_cpu:
@@ -875,7 +875,7 @@ def run_gpu(args):
     e1.synchronize()
     t_mix_warm = e0.elapsed_time(e1) / 1e3 / 50
     hbm, peak_kind = peaks()
-    B_mix = 28 * nblk + 4 * (A.n_slices + 1) + 16 * N
+    B_mix = 32 * nblk + 4 * (A.n_slices + 1) + 16 * N
     B_csr = 12 * nnz + 4 * (N + 1) + 8 * N + 8 * N
     B_b64 = 36 * nblk + 4 * (A.n_slices + 1) + 16 * N
     B_b32 = 20 * nblk + 4 * (A.n_slices + 1) + 8 * N
@@ -895,9 +895,9 @@ def run_gpu(args):
 
     # ---- roofline of the mixed solver kernel: algorithmic bytes per iteration,
     # counting each array the fused schedule moves through HBM once, in the
-    # format it reads.  Matrix stream per 2x2 block: FP32 values (16 B), 16-bit
-    # remainders (8 B), column (4 B), plus the slice offsets.  The block's own
-    # rows of x, r, w and p live in shared memory for the whole solve; the
+    # format it reads.  Matrix stream per 2x2 block: FP32 values (16 B), 23-bit
+    # remainders (8 + 4 B), column (4 B), plus the slice offsets.  The block's
+    # own rows of x, r, w and p live in shared memory for the whole solve; the
     # search direction p crosses HBM (written as FP32 hi + lo, 8 B/dof, in L3
     # and gathered, 8 B/dof, by the next SpMV) and 1/Aii (4 B/dof) is read in
     # L2 and L3.  A reliable update reads the FP64 matrix (32 B values + 4 B
@@ -906,15 +906,15 @@ def run_gpu(args):
     t_med = float(np.median(t_mixed))
     form = mixed_form
     if form == 2:
-        # ghost-node form: 26 B per block (16-bit local column), and per dof r
-        # published (4 B), x in and out (16 B), 1/Aii in L2 and L3 (8 B), plus
-        # r and 1/Aii of every block's ghosts (8 B per ghost dof)
+        # ghost-node form: 30 B per block (16-bit local column), and per dof r
+        # published (hi and lo, 8 B), x in and out (16 B), 1/Aii in L2 and L3
+        # (8 B), plus r and 1/Aii of every block's ghosts (12 B per ghost dof)
         ghost_dofs = 2 * ghost_count(s.get(L.FEM_ROW_PTR), s.get(L.FEM_COL_IDX), A.n_slices,
                                      mixed_blocks(A.n_slices, dev))
-        bytes_iter = 26 * nblk + 4 * (A.n_slices + 1) + 28 * N + 8 * ghost_dofs
+        bytes_iter = 30 * nblk + 4 * (A.n_slices + 1) + 32 * N + 12 * ghost_dofs
     else:
         ghost_dofs = 0
-        bytes_iter = 28 * nblk + 4 * (A.n_slices + 1) + 24 * N
+        bytes_iter = 32 * nblk + 4 * (A.n_slices + 1) + 24 * N
     upd_bytes = (r_mixed.n_updates + 1) * (36 * nblk + 4 * (A.n_slices + 1) + 24 * N)
     achieved = (bytes_iter * it + upd_bytes) / t_med / 1e9
     # fast FP64 kernel (vectors in global memory): 36 B per block, and per dof

@@ -218,10 +218,11 @@ int nbg_cg_f64_noalloc(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_
 /* Device arrays of the node-block layout of a CSR from nb_sparse_create(.., 2)
  * (two rows per node with the same (2w, 2w+1) column pairs, sparse.c:36-52):
  * entry (slice s, k, lane r) sits at (slice_off[s] + k) * 32 + r; b64 holds
- * 4 doubles (a00 a01 a10 a11) per entry, b32 the same rounded to float and
- * blo the remainders (double - float) as 16-bit counts q + 32768 of units
- * of 2^-39 float (|q| <= 32767), so that b32 + blo carries about 40
- * significant bits in 6 bytes; dinv = 1 / diagonal per scalar row.  Any array may be NULL when a
+ * 4 doubles (a00 a01 a10 a11) per entry, b32 the same rounded to float, and
+ * the remainders (double - float) as biased 23-bit counts q + 2^22 of units
+ * of 2^-46 float (|q| < 2^22): their low 16 bits in blo, their high 7 bits
+ * in bxt, so that b32 + blo + bxt carries about 47 significant bits in 7
+ * bytes; dinv = 1 / diagonal per scalar row.  Any array may be NULL when a
  * caller does not need it. */
 typedef struct {
     uint32_t N;            /* scalar rows (= 2 Nn) */
@@ -232,7 +233,8 @@ typedef struct {
     const uint32_t *bcol;
     const double *b64;
     const float *b32;
-    const uint16_t *blo;   /* 4 remainder counts per entry */
+    const uint16_t *blo;   /* low 16 bits of the 4 remainder counts per entry */
+    const uint8_t *bxt;    /* their high 7 bits, one byte each */
     const double *dinv64;
     const float *dinv32;
     /* Optional node order (device, NULL = identity): slice row i holds node

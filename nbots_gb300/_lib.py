@@ -34,7 +34,7 @@ class MixedResult(C.Structure):
 
 class Bsr(C.Structure):
     _fields_ = [("N", u32), ("Nn", u32), ("n_slices", u32), ("n_entries", u64),
-                ("slice_off", vp), ("bcol", vp), ("b64", vp), ("b32", vp), ("blo", vp), ("dinv64", vp),
+                ("slice_off", vp), ("bcol", vp), ("b64", vp), ("b32", vp), ("blo", vp), ("bxt", vp), ("dinv64", vp),
                 ("dinv32", vp), ("perm", vp), ("iperm", vp)]
 
 

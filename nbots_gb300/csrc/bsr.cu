@@ -27,7 +27,8 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
                            const uint32_t* __restrict__ perm, const uint32_t* __restrict__ iperm,
                            uint32_t* __restrict__ bcol, double* __restrict__ b64,
                            float* __restrict__ b32, uint16_t* __restrict__ blo,
-                           double* __restrict__ dinv64, float* __restrict__ dinv32) {
+                           uint8_t* __restrict__ bxt, double* __restrict__ dinv64,
+                           float* __restrict__ dinv32) {
     const uint32_t i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= Nn) return;
     const uint32_t s = i >> 5, lane = i & 31;
@@ -61,16 +62,16 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
         }
         const float h00 = (float)a00, h01 = (float)a01, h10 = (float)a10, h11 = (float)a11;
         if (b32) reinterpret_cast<float4*>(b32)[e] = make_float4(h00, h01, h10, h11);
-        if (blo) {
-            // remainders (exact in FP64) as biased 16-bit counts of 2^-39 hi
-            const uint16_t q0 = rem16_encode(a00, h00);
-            const uint16_t q1 = rem16_encode(a01, h01);
-            const uint16_t q2 = rem16_encode(a10, h10);
-            const uint16_t q3 = rem16_encode(a11, h11);
+        if (blo && bxt) {
+            // remainders (exact in FP64) as biased 23-bit counts of 2^-46 hi
+            const uint32_t q0 = rem23_encode(a00, h00), q1 = rem23_encode(a01, h01);
+            const uint32_t q2 = rem23_encode(a10, h10), q3 = rem23_encode(a11, h11);
             uint2 packed;
-            packed.x = (uint32_t)q0 | ((uint32_t)q1 << 16);
-            packed.y = (uint32_t)q2 | ((uint32_t)q3 << 16);
+            packed.x = (q0 & 0xFFFFu) | (q1 << 16);
+            packed.y = (q2 & 0xFFFFu) | (q3 << 16);
             reinterpret_cast<uint2*>(blo)[e] = packed;
+            reinterpret_cast<uint32_t*>(bxt)[e] =
+                (q0 >> 16) | ((q1 >> 16) << 8) | ((q2 >> 16) << 16) | ((q3 >> 16) << 24);
         }
     }
     if (dinv64) {
@@ -166,8 +167,8 @@ extern "C" int nbg_bsr_fill(const nbg_bsr_t* A, const uint32_t* row_ptr, const u
     if ((A->perm == nullptr) != (A->iperm == nullptr)) return NBG_ERR_ARG;
     k_bsr_fill<<<(A->Nn + 255) / 256, 256, 0, (cudaStream_t)stream>>>(
         A->Nn, row_ptr, col_idx, val, A->slice_off, A->perm, A->iperm, (uint32_t*)A->bcol,
-        (double*)A->b64, (float*)A->b32, (uint16_t*)A->blo, (double*)A->dinv64,
-        (float*)A->dinv32);
+        (double*)A->b64, (float*)A->b32, (uint16_t*)A->blo, (uint8_t*)A->bxt,
+        (double*)A->dinv64, (float*)A->dinv32);
     NBG_CHECK(cudaGetLastError());
     return NBG_OK;
 }

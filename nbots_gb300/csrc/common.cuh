@@ -238,7 +238,7 @@ struct FFAcc {
         c = __fadd_rn(c, __fadd_rn(t.lo, e));
     }
     // (ahi + s ahi)(xhi + xlo) with the remainder given by its scale s
-    // (rem16_scale): the term s ahi xhi uses the rounded product ahi xhi.
+    // (rem23_scale): the term s ahi xhi uses the rounded product ahi xhi.
     __device__ __forceinline__ void fma2s(float ahi, float sc, float xhi, float xlo) {
         FF p = two_prod(ahi, xhi);
         float e = __fmaf_rn(ahi, xlo, p.lo);
@@ -261,34 +261,43 @@ __device__ __forceinline__ FF ff_add(FF a, FF b) {
     return fast_two_sum(s.hi, __fadd_rn(s.lo, __fadd_rn(a.lo, b.lo)));
 }
 
-// Remainder a - hi of an FP32 rounding hi = fl(a), stored in 16 bits as
-// the biased count q + 32768 of units of 2^-39 hi (|a - hi| <= 2^-24 |hi|,
-// so |q| <= 2^15, clamped to 32767): hi + lo then carries about 40
-// significant bits in 6 bytes.  Decoding needs no conversion instruction:
-// the count placed in the mantissa of a float with exponent -16 is
-// 2^-16 + (q + 32768) 2^-39, and subtracting 2^-16 + 2^-24 (exact) leaves
-// s = q 2^-39, with lo = s hi.
-__device__ __forceinline__ uint16_t rem16_encode(double a, float hi) {
-    if (hi == 0.f) return 32768;
-    double q = rint((a - (double)hi) / ((double)hi * 0x1p-39));
-    q = q > 32767.0 ? 32767.0 : (q < -32767.0 ? -32767.0 : q);
-    return (uint16_t)((int)q + 32768);
+// Remainder a - hi of an FP32 rounding hi = fl(a), stored as the biased
+// count c = q + 2^22 of units of 2^-46 hi (|a - hi| <= 2^-24 |hi|, so
+// |q| <= 2^22, clamped to 2^22 - 1): its low 16 bits in one array (blo),
+// its high 7 bits in a byte of another (bxt).  hi + lo then carries about
+// 47 significant bits in 7 bytes.  With 16-bit counts (about 40 bits) the
+// iteration counts matched FP64 but the mixed solution kept an error of
+// 1e-8 to 1e-7 in the smooth modes that its residual barely sees (a CPU
+// emulation of the solver on the same cantilever: 1.3e-8 at 512x256,
+// 4.9e-10 with 20-bit counts, 3.1e-10 with these, FP64's 3.1e-10).
+// Decoding needs no conversion instruction: c placed in the mantissa of a
+// float with exponent -23 is 2^-23 + c 2^-46, and subtracting
+// 2^-23 + 2^-24 (exact: both within one binade) leaves s = q 2^-46, with
+// lo = s hi.
+__device__ __forceinline__ uint32_t rem23_encode(double a, float hi) {
+    if (hi == 0.f) return 1u << 22;
+    double q = rint((a - (double)hi) / ((double)hi * 0x1p-46));
+    const double lim = (double)((1 << 22) - 1);
+    q = q > lim ? lim : (q < -lim ? -lim : q);
+    return (uint32_t)((int)q + (1 << 22));
 }
 
-// s = q 2^-39 for the biased count in the low (hi16 = false) or high half
-// of v: one byte permute and one subtraction.
-__device__ __forceinline__ float rem16_scale(uint32_t v, bool hi16) {
-    uint32_t bits;
-    // bytes 0, 1 of the result from v's low or high half, bytes 2, 3 = 0x80, 0x37
-    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(bits) : "r"(v), "r"(0x37800000u),
-        "r"(hi16 ? 0x7632u : 0x7610u));
-    return __fsub_rn(__uint_as_float(bits), 0x1.01p-16f);
+// s = q 2^-46 for the count whose low 16 bits are bytes j0, j0 + 1 of lo and
+// whose high 7 bits are byte 4 + jx of {lo, ext} (prmt numbering): one byte
+// permute, one logic operation and one subtraction.
+template <uint32_t kSel>
+__device__ __forceinline__ float rem23_scale(uint32_t lo, uint32_t ext) {
+    uint32_t t;
+    asm("prmt.b32 %0, %1, %2, %3;" : "=r"(t) : "r"(lo), "r"(ext), "n"(kSel));
+    // byte 3: sign 0 and the exponent's top 7 bits (-23 + 127 = 0x68)
+    return __fsub_rn(__uint_as_float((t & 0x00FFFFFFu) | 0x34000000u), 0x1.8p-23f);
 }
 
-// The four scales of one 2x2 block (packed counts).
-__device__ __forceinline__ float4 rem16_scale4(uint2 v) {
-    return make_float4(rem16_scale(v.x, false), rem16_scale(v.x, true), rem16_scale(v.y, false),
-                       rem16_scale(v.y, true));
+// The four scales of one 2x2 block: the low halves packed two per word of
+// lo, the high parts one per byte of ext.
+__device__ __forceinline__ float4 rem23_scale4(uint2 lo, uint32_t ext) {
+    return make_float4(rem23_scale<0x0410>(lo.x, ext), rem23_scale<0x0532>(lo.x, ext),
+                       rem23_scale<0x0610>(lo.y, ext), rem23_scale<0x0732>(lo.y, ext));
 }
 
 // a * b, both float-float
@@ -297,6 +306,23 @@ __device__ __forceinline__ FF ff_mul(FF a, FF b) {
     float e = __fmaf_rn(a.hi, b.lo, p.lo);
     e = __fmaf_rn(a.lo, b.hi, e);
     return fast_two_sum(p.hi, e);
+}
+
+// a * b for a float-float a and an FP32 b
+__device__ __forceinline__ FF ff_mulf(FF a, float b) {
+    const FF p = two_prod(a.hi, b);
+    return fast_two_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
+}
+
+// a / b, both float-float, by Dekker's long division (1971): the FP32
+// quotient q1 of the leading parts, the remainder a - q1 b in float-float,
+// and a second FP32 quotient of the remainder.  About 44 significant bits,
+// all on the FP32 pipe.
+__device__ __forceinline__ FF ff_div(FF a, FF b) {
+    const float q1 = __fdiv_rn(a.hi, b.hi);
+    const FF p = ff_mul(FF{q1, 0.f}, b);
+    const FF r = ff_add(a, FF{-p.hi, -p.lo});
+    return fast_two_sum(q1, __fdiv_rn(r.hi, b.hi));
 }
 
 // Rows row0 .. row0 + nrows - 1 (nrows <= 32) of a CSR matrix times x in

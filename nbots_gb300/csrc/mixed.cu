@@ -6,25 +6,32 @@
 // (1M dof), the inflation comes from three places: the precision of the
 // matrix values (even 32 significant bits cost 1.33x the iterations: the
 // inner operator must match the FP64 one behind the residual), FP32 search
-// directions p and FP32 products A p, and an FP32 correction x.  The FP32
-// residual r is harmless.  So the inner iteration runs on the FP32 pipes
-// with:
-//   matrix      FP32 hi + a 16-bit remainder in units of 2^-39 hi
-//               (about 40 significant bits in 6 B/value instead of 8),
+// directions p and FP32 products A p, and an FP32 correction x.  The
+// iteration count alone is not the whole story: with about 40-bit matrix
+// values and an FP32 residual the counts match FP64, yet the solution
+// keeps an error of 1e-8 to 1e-7 (varying with rounding details) in the
+// smooth modes, whose share of the residual is too small for the stopping
+// test to see.  A CPU emulation of this solver on the cantilever traced it
+// to the FP32 residual (its rounding each iteration feeds those modes) and
+// to the matrix precision; with both raised the error matches FP64's.  So
+// the inner iteration runs on the FP32 pipes with:
+//   matrix      FP32 hi + a 23-bit remainder in units of 2^-46 hi
+//               (about 47 significant bits in 7 B/value instead of 8),
 //   p, A p      FP32 hi + FP32 lo per dof (float-float),
-//   x           float-float (FP32 hi + FP32 lo),
-//   r           FP32,
+//   x, r        float-float,
 // products and sums by error-free transformations (TwoProduct with FMA,
-// TwoSum), dot products with compensated FP32 sums per thread and FP64
-// across threads.  A reliable update (Sleijpen & van der Vorst 1996) adds x
-// to the FP64 solution and recomputes r = b - A u in FP64 with the FP64
-// values whenever |r| has fallen by `delta` since the last one; p is kept,
-// so the Krylov progress survives.  Convergence is judged on the FP64
-// residual only.  Three grid barriers per iteration (L1 | L2 | L3 of
-// cg_precond_jacobi.c:50-74): folding L3 into the next SpMV (each block
-// rebuilding z + beta p for the columns it reads) measured slower, 77 vs
-// 66 us per iteration at 1M dof, because the float-float rebuild per column
-// costs more issue slots and gather bytes than the barrier it saves.
+// TwoSum), dot products with compensated FP32 sums per thread and
+// float-float sums across threads and blocks.  A reliable update (Sleijpen
+// & van der Vorst 1996) adds x to the FP64 solution and recomputes
+// r = b - A u in FP64 with the FP64 values whenever |r| has fallen by
+// `delta` since the last one; p is kept, so the Krylov progress survives.
+// Convergence is judged on the FP64 residual only.  Three grid barriers per
+// iteration in the global-gather form (L1 | L2 | L3 of
+// cg_precond_jacobi.c:50-74), two in the ghost-node form below: folding L3
+// into the next SpMV (each block rebuilding z + beta p for the columns it
+// reads) measured slower, 77 vs 66 us per iteration at 1M dof, because the
+// float-float rebuild per column costs more issue slots and gather bytes
+// than the barrier it saves.
 #include <algorithm>
 #include <cmath>
 #include <cstdint>
@@ -120,9 +127,9 @@ using LoW = LoBF;
 #define NBG_MIXED_DV_SHARED 0
 #endif
 constexpr bool kDvShared = NBG_MIXED_DV_SHARED;
-// own-row bytes per node: x (hi, lo), r, A p hi, p hi (8 B each), 1/Aii
-// (8 B, when shared) and the low pairs
-constexpr size_t kOwnNodeBytes = 40 + (kDvShared ? 8 : 0) + sizeof(LoP::two) + sizeof(LoW::two);
+// own-row bytes per node: x (hi, lo), r (hi, lo), A p hi, p hi (8 B each),
+// 1/Aii (8 B, when shared) and the low pairs
+constexpr size_t kOwnNodeBytes = 48 + (kDvShared ? 8 : 0) + sizeof(LoP::two) + sizeof(LoW::two);
 
 struct MixArgs {
     nbg_bsr_t A;
@@ -131,6 +138,7 @@ struct MixArgs {
     float* ph;               // search direction, global (gathered by neighbours)
     LoP::one* pl;
     float *r, *wh, *xh, *xl;  // own-row vectors when they do not fit in shared memory
+    float* rl;                // low part of r (float-float residual)
     LoW::one* wl;
     uint32_t max_iter;
     double tol, delta;
@@ -152,6 +160,70 @@ struct Group {
 
 
 
+// Scalar state of one solve, kept by thread 0 of every block of the group
+// (each block derives the same values from the same partial sums).  Per
+// iteration it runs on the FP32 pipes: p.w, r.z and |r|^2 arrive as
+// float-float sums, the step lengths are float-float quotients (ff_div) and
+// the update test compares FP32 leading parts.  GB300 issues FP64 at a small
+// fraction of its FP32 rate: one FP64 division on thread 0 held its block
+// for about half a microsecond, twice per iteration.  FP64 stays where the
+// result is judged, on the true residual at the start and at each reliable
+// update.
+struct MixScalars {
+    FF rz;                          // r.z of the current residual
+    double rr64, bb, target2;       // true |r|^2, |b|^2, stopping threshold
+    float rmax2, target2f, delta2;  // update test
+    uint32_t k, nupd;
+    int converged;
+
+    __device__ __forceinline__ void clear() {
+        rz = FF{0.f, 0.f};
+        rr64 = bb = target2 = 0.0;
+        rmax2 = target2f = delta2 = 0.f;
+        k = nupd = 0;
+        converged = 0;
+    }
+    // The start's sums {|r|^2, |b|^2, r.z} (FP64): 2 stop, 0 iterate.
+    __device__ __forceinline__ int start(const double (&t)[3], const MixArgs& a) {
+        rr64 = t[0];
+        bb = t[1];
+        rz = ff_from_double(t[2]);
+        target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * bb : a.tol * a.tol;
+        target2f = (float)target2;
+        delta2 = (float)(a.delta * a.delta);
+        rmax2 = (float)rr64;
+        converged = !(rr64 > target2);
+        return (converged || a.max_iter == 0) ? 2 : 0;
+    }
+    __device__ __forceinline__ FF alpha(FF pw) const { return ff_div(rz, pw); }
+    // The recursive residual's {r.z, |r|^2}: 1 when a reliable update is
+    // due, else 0 with beta.
+    __device__ __forceinline__ int step(FF rz_new, FF rr, uint32_t max_iter, FF& beta) {
+        if (rr.hi > rmax2) rmax2 = rr.hi;
+        k++;
+        const int upd = rr.hi <= delta2 * rmax2 || rr.hi <= target2f || k >= max_iter;
+        if (!upd) {
+            beta = ff_div(rz_new, rz);
+            rz = rz_new;
+        }
+        return upd;
+    }
+    // A reliable update's {|r|^2, r.z} (FP64): 2 stop, else 0 with beta.
+    __device__ __forceinline__ int replaced(const double (&t)[2], uint32_t max_iter, FF& beta) {
+        rr64 = t[0];
+        rmax2 = (float)rr64;
+        nupd++;
+        converged = !(rr64 > target2);
+        const int stop = converged || k >= max_iter;
+        if (!stop) {
+            const FF rzn = ff_from_double(t[1]);
+            beta = ff_div(rzn, rz);
+            rz = rzn;
+        }
+        return stop ? 2 : 0;
+    }
+};
+
 // Half of w = A p for node row (s, r): lanes l and l + 16 share row
 // r = 16 h + (l & 15) of slice s, taking alternate entries, so a warp works on
 // half a slice at a time (the block's 2 (s1 - s0) half slices spread evenly
@@ -164,6 +236,7 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
                                                 FF& y1) {
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
+    const uint32_t* __restrict__ bx = reinterpret_cast<const uint32_t*>(a.A.bxt);
     const float2* __restrict__ ph = reinterpret_cast<const float2*>(a.ph);
     const LoP::two* __restrict__ pl = reinterpret_cast<const LoP::two*>(a.pl);
     FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
@@ -175,7 +248,7 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
         const size_t e = (size_t)k * 32 + r;
         const uint32_t c = ld_hint(a.A.bcol + e, pol);
         const float4 m = ld_hint(bh + e, pol);
-        const float4 sc = rem16_scale4(ld_hint(bl + e, pol));
+        const float4 sc = rem23_scale4(ld_hint(bl + e, pol), ld_hint(bx + e, pol));
         const float2 pc = ph[c];
         const float2 pcl = LoP::unpack(pl[c]);
         c0.fma2s(m.x, sc.x, pc.x, pcl.x);
@@ -197,7 +270,7 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
 // Own-row vectors of this block, indexed by local node row
 // (i - 32 * s0): shared memory when they fit, else the global workspace.
 struct Own {
-    float2 *xh, *xl, *r, *dv, *wh, *ph;
+    float2 *xh, *xl, *r, *rl, *dv, *wh, *ph;
     LoW::two* wl;
     LoP::two* pl;
 };
@@ -214,7 +287,8 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
         o.r = f + 2 * nrows;
         o.wh = f + 3 * nrows;
         o.ph = f + 4 * nrows;
-        f += 5 * nrows;
+        o.rl = f + 5 * nrows;
+        f += 6 * nrows;
         if (kDvShared) {
             o.dv = f;
             f += nrows;
@@ -227,6 +301,7 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
         o.xh = reinterpret_cast<float2*>(a.xh) + base;
         o.xl = reinterpret_cast<float2*>(a.xl) + base;
         o.r = reinterpret_cast<float2*>(a.r) + base;
+        o.rl = reinterpret_cast<float2*>(a.rl) + base;
         o.dv = const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) + base;
         o.wh = reinterpret_cast<float2*>(a.wh) + base;
         o.ph = reinterpret_cast<float2*>(a.ph) + base;
@@ -236,7 +311,7 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
     return o;
 }
 
-// r = b - A u in FP64 for the own rows, stored as FP32; z = r / Aii
+// r = b - A u in FP64 for the own rows, stored as float-float; z = r / Aii
 // (float-float); accumulates |r|^2 (FP64), r.z and optionally |b|^2; with
 // set_p, p = z (own copy and the global one).
 template <int kThreads>
@@ -255,12 +330,13 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
         const double r0 = bi.x - au.x, r1 = bi.y - au.y;
         rr = fma(r0, r0, fma(r1, r1, rr));
         if (bb) *bb = fma(bi.x, bi.x, fma(bi.y, bi.y, *bb));
-        const float f0 = (float)r0, f1 = (float)r1;
-        o.r[li] = make_float2(f0, f1);
+        const FF f0 = ff_from_double(r0), f1 = ff_from_double(r1);
+        o.r[li] = make_float2(f0.hi, f1.hi);
+        o.rl[li] = make_float2(f0.lo, f1.lo);
         const float2 di = o.dv[li];
-        const FF z0 = two_prod(f0, di.x), z1 = two_prod(f1, di.y);
-        rz.fma2(f0, 0.f, z0.hi, z0.lo);
-        rz.fma2(f1, 0.f, z1.hi, z1.lo);
+        const FF z0 = ff_mulf(f0, di.x), z1 = ff_mulf(f1, di.y);
+        rz.fma2(f0.hi, f0.lo, z0.hi, z0.lo);
+        rz.fma2(f1.hi, f1.lo, z1.hi, z1.lo);
         if (set_p) {
             const float2 hi = make_float2(z0.hi, z1.hi);
             const LoP::two lo = LoP::pack(z0.lo, z1.lo);
@@ -275,8 +351,8 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
 // The solver of one system on the blocks [g_base, g_base + g_size) of the
 // launch: its own slices, group barrier, partial sums and result.  The
 // scalar recurrences (step lengths, residual norms, stopping and update
-// decisions) run in thread 0 in FP64 and reach the block through shared
-// memory as FP32 pairs and flags.
+// decisions) run in thread 0 (MixScalars) and reach the block through
+// shared memory as FP32 pairs and flags.
 template <bool kRes, int kThreads>
 __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, unsigned char* smem) {
     // batched launches give each system at most a few dozen blocks
@@ -285,11 +361,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     float2* const ffred = reinterpret_cast<float2*>(red);
     __shared__ float s_alpha[2], s_beta[2];
     __shared__ int s_flag;  // 0 iterate, 1 reliable update, 2 stop
-    __shared__ struct {
-        double rz, rmax2, rr64, bb, target2;
-        uint32_t k, nupd;
-        int converged;
-    } sc;  // scalar state, thread 0 only
+    __shared__ MixScalars sc;  // thread 0 only
     const unsigned G = g.g_size;
     const uint32_t rank = blockIdx.x - g.g_base;
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -305,11 +377,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     double* const part2 = g.part + 3 * g.pstride;
     auto sync = [&]() { return grid_barrier(g.bar, G, rank, g.status); };
 
-    if (threadIdx.x == 0) {
-        sc.rz = sc.rmax2 = sc.rr64 = sc.bb = sc.target2 = 0.0;
-        sc.k = sc.nupd = 0;
-        sc.converged = 0;
-    }
+    if (threadIdx.x == 0) sc.clear();
     {   // init: own copy of 1/Aii, x = 0, r = b - A u (FP64), p = z
         const float2* __restrict__ gdv = reinterpret_cast<const float2*>(a.A.dinv32);
         for (uint32_t s = s0 + warp; s < s1; s += nw) {
@@ -331,15 +399,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     {
         double t[3];
         group_reduce0<3>(part2, G, t);
-        if (threadIdx.x == 0) {
-            sc.rr64 = t[0];
-            sc.bb = t[1];
-            sc.rz = t[2];
-            sc.target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * sc.bb : a.tol * a.tol;
-            sc.rmax2 = sc.rr64;
-            sc.converged = !(sc.rr64 > sc.target2);
-            s_flag = (sc.converged || a.max_iter == 0) ? 2 : 0;
-        }
+        if (threadIdx.x == 0) s_flag = sc.start(t, a);
         __syncthreads();
     }
     while (s_flag != 2) {
@@ -370,10 +430,10 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
         }
         if (sync()) goto done;
         {
-            double pwd[1];
-            group_reduce0_ff<1, kRB>(reinterpret_cast<const float2*>(part0), G, pwd);
+            FF pw[1];
+            group_reduce0_ff<1, kRB>(reinterpret_cast<const float2*>(part0), G, pw);
             if (threadIdx.x == 0) {
-                const FF al = ff_from_double(sc.rz / pwd[0]);
+                const FF al = sc.alpha(pw[0]);
                 s_alpha[0] = al.hi;
                 s_alpha[1] = al.lo;
             }
@@ -388,42 +448,36 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
                 const float2 p = o.ph[li], plo = LoP::unpack(o.pl[li]);
                 const float2 w = o.wh[li], wlo = LoW::unpack(o.wl[li]);
                 const float2 xhi = o.xh[li], xlo = o.xl[li];
-                const float2 ri = o.r[li], di = o.dv[li];
+                const float2 ri = o.r[li], rli = o.rl[li], di = o.dv[li];
                 const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, plo.x}));
                 const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, plo.y}));
                 o.xh[li] = make_float2(x0.hi, x1.hi);
                 o.xl[li] = make_float2(x0.lo, x1.lo);
                 const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
-                const FF t0 = two_sum(ri.x, -aw0.hi), t1 = two_sum(ri.y, -aw1.hi);
-                const float r0 = __fadd_rn(t0.hi, __fsub_rn(t0.lo, aw0.lo));
-                const float r1 = __fadd_rn(t1.hi, __fsub_rn(t1.lo, aw1.lo));
-                o.r[li] = make_float2(r0, r1);
-                const FF z0 = two_prod(r0, di.x), z1 = two_prod(r1, di.y);
-                rzk.fma2(r0, 0.f, z0.hi, z0.lo);
-                rzk.fma2(r1, 0.f, z1.hi, z1.lo);
-                rrk.fma2(r0, 0.f, r0, 0.f);
-                rrk.fma2(r1, 0.f, r1, 0.f);
+                const FF r0 = ff_add({ri.x, rli.x}, {-aw0.hi, -aw0.lo});
+                const FF r1 = ff_add({ri.y, rli.y}, {-aw1.hi, -aw1.lo});
+                o.r[li] = make_float2(r0.hi, r1.hi);
+                o.rl[li] = make_float2(r0.lo, r1.lo);
+                const FF z0 = ff_mulf(r0, di.x), z1 = ff_mulf(r1, di.y);
+                rzk.fma2(r0.hi, r0.lo, z0.hi, z0.lo);
+                rzk.fma2(r1.hi, r1.lo, z1.hi, z1.lo);
+                rrk.fma2(r0.hi, r0.lo, r0.hi, r0.lo);
+                rrk.fma2(r1.hi, r1.lo, r1.hi, r1.lo);
             }
             FF v[2] = {rzk.result(), rrk.result()};
             group_publish_ff<2>(v, ffred, reinterpret_cast<float2*>(part1), rank);
         }
         if (sync()) goto done;
         {
-            double t2[2];
+            FF t2[2];
             group_reduce0_ff<2, kRB>(reinterpret_cast<const float2*>(part1), G, t2);
             if (threadIdx.x == 0) {
-                const double rz_new = t2[0], rr = t2[1];
-                if (rr > sc.rmax2) sc.rmax2 = rr;
-                sc.k++;
-                const int upd = rr <= a.delta * a.delta * sc.rmax2 || rr <= sc.target2 ||
-                                sc.k >= a.max_iter;
-                if (!upd) {
-                    const FF be = ff_from_double(rz_new / sc.rz);
-                    sc.rz = rz_new;
+                FF be;
+                s_flag = sc.step(t2[0], t2[1], a.max_iter, be);
+                if (!s_flag) {
                     s_beta[0] = be.hi;
                     s_beta[1] = be.lo;
                 }
-                s_flag = upd;
             }
             __syncthreads();
         }
@@ -452,18 +506,12 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             double tt[2];
             group_reduce0<2>(part2, G, tt);
             if (threadIdx.x == 0) {
-                sc.rr64 = tt[0];
-                sc.rmax2 = sc.rr64;
-                sc.nupd++;
-                sc.converged = !(sc.rr64 > sc.target2);
-                const int stop = sc.converged || sc.k >= a.max_iter;
-                if (!stop) {
-                    const FF be = ff_from_double(tt[1] / sc.rz);
-                    sc.rz = tt[1];
+                FF be;
+                s_flag = sc.replaced(tt, a.max_iter, be);
+                if (!s_flag) {
                     s_beta[0] = be.hi;
                     s_beta[1] = be.lo;
                 }
-                s_flag = stop ? 2 : 0;
             }
             __syncthreads();
             if (s_flag == 2) break;
@@ -473,10 +521,10 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
-                const float2 ri = o.r[li], di = o.dv[li];
+                const float2 ri = o.r[li], rli = o.rl[li], di = o.dv[li];
                 const float2 p = o.ph[li], plo = LoP::unpack(o.pl[li]);
-                const FF n0 = ff_add(two_prod(ri.x, di.x), ff_mul(beta, {p.x, plo.x}));
-                const FF n1 = ff_add(two_prod(ri.y, di.y), ff_mul(beta, {p.y, plo.y}));
+                const FF n0 = ff_add(ff_mulf({ri.x, rli.x}, di.x), ff_mul(beta, {p.x, plo.x}));
+                const FF n1 = ff_add(ff_mulf({ri.y, rli.y}, di.y), ff_mul(beta, {p.y, plo.y}));
                 const float2 hi = make_float2(n0.hi, n1.hi);
                 const LoP::two lo = LoP::pack(n0.lo, n1.lo);
                 if (kRes) {
@@ -541,10 +589,10 @@ __global__ void __launch_bounds__(kBatThreads, kBatMinBlocks)
 }
 
 // Share of the SpMV's matrix stream (FP32 values, remainders, columns:
-// 28 B per block entry) marked evict_last: what fits in NBG_L2_KEEP percent
+// 32 B per block entry) marked evict_last: what fits in NBG_L2_KEEP percent
 // of this device's L2, the rest of L2 being left to the gathered vector and
 // the other data.
-uint32_t keep_permille(const nbg_bsr_t& A, double bytes_per_entry = 28.0) {
+uint32_t keep_permille(const nbg_bsr_t& A, double bytes_per_entry = 32.0) {
     int dev = 0, l2 = 0;
     if (cudaGetDevice(&dev) != cudaSuccess ||
         cudaDeviceGetAttribute(&l2, cudaDevAttrL2CacheSize, dev) != cudaSuccess)
@@ -557,7 +605,7 @@ uint32_t keep_permille(const nbg_bsr_t& A, double bytes_per_entry = 28.0) {
 
 size_t mixed_core_bytes(uint32_t N) {
     const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
-    return 5 * f + 2 * h + align256(kMaxBlocks * 6 * 8) + 3 * 256;
+    return 6 * f + 2 * h + align256(kMaxBlocks * 6 * 8) + 3 * 256;
 }
 
 // plus the permuted copies of b and x for a layout with a node order
@@ -596,7 +644,7 @@ __global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
 // its ghosts in shared memory, with the layout's columns renumbered locally
 // in 16 bits (own row slots first, then the ghosts in ascending node order),
 // so the SpMV gathers from shared memory, not L2, and the matrix stream is
-// 26 B per block entry instead of 28.  Owners publish their FP32 residual r
+// 30 B per block entry instead of 32.  Owners publish their residual r
 // (after L2 and after each reliable update); after the barrier that ends L2
 // every block computes its ghosts' new p itself, with the owner's arithmetic
 // on the owner's r and on its own copy of the ghost's previous p (the same
@@ -744,6 +792,7 @@ __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t
                                                 uint64_t pol, FF& y0, FF& y1) {
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
+    const uint32_t* __restrict__ bx = reinterpret_cast<const uint32_t*>(a.A.bxt);
     FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
     // so: this block's slice offsets, so[0] that of its first slice
     const uint32_t k0 = so[s] + par, k1 = live ? so[s + 1] : 0;
@@ -752,7 +801,7 @@ __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t
         const size_t e = (size_t)k * 32 + r;
         const uint32_t c = ld_hint(lcol + e, pol);
         const float4 m = ld_hint(bh + e, pol);
-        const float4 sc = rem16_scale4(ld_hint(bl + e, pol));
+        const float4 sc = rem23_scale4(ld_hint(bl + e, pol), ld_hint(bx + e, pol));
         const float4 pv = P[c];
         c0.fma2s(m.x, sc.x, pv.x, pv.z);
         c0.fma2s(m.y, sc.y, pv.y, pv.w);
@@ -770,10 +819,11 @@ __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t
     y1 = t[1];
 }
 
-// true_residual for the ghost form: r to shared memory and published to
-// global memory for the blocks that hold this row as a ghost.
+// true_residual for the ghost form: r (float-float) to global memory, its
+// hi and lo arrays, where the owner keeps it and the blocks that hold this
+// row as a ghost read it.
 template <int kThreads>
-__device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float2* R, float4* P,
+__device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float4* P,
                                                     uint32_t s0, uint32_t s1, double& rr,
                                                     FFAcc& rz, double* bb, bool set_p) {
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -782,6 +832,7 @@ __device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float2* R,
     const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
     const float2* __restrict__ dinv = reinterpret_cast<const float2*>(a.A.dinv32);
     float2* __restrict__ gr = reinterpret_cast<float2*>(a.r);
+    float2* __restrict__ grl = reinterpret_cast<float2*>(a.rl);
     for (uint32_t s = s0 + warp; s < s1; s += nw) {
         const uint32_t i = s * 32 + lane, li = i - s0 * 32;
         if (i >= a.A.Nn) continue;
@@ -790,13 +841,13 @@ __device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float2* R,
         const double r0 = bi.x - au.x, r1 = bi.y - au.y;
         rr = fma(r0, r0, fma(r1, r1, rr));
         if (bb) *bb = fma(bi.x, bi.x, fma(bi.y, bi.y, *bb));
-        const float f0 = (float)r0, f1 = (float)r1;
-        R[li] = make_float2(f0, f1);
-        gr[i] = make_float2(f0, f1);
+        const FF f0 = ff_from_double(r0), f1 = ff_from_double(r1);
+        gr[i] = make_float2(f0.hi, f1.hi);
+        grl[i] = make_float2(f0.lo, f1.lo);
         const float2 di = dinv[i];
-        const FF z0 = two_prod(f0, di.x), z1 = two_prod(f1, di.y);
-        rz.fma2(f0, 0.f, z0.hi, z0.lo);
-        rz.fma2(f1, 0.f, z1.hi, z1.lo);
+        const FF z0 = ff_mulf(f0, di.x), z1 = ff_mulf(f1, di.y);
+        rz.fma2(f0.hi, f0.lo, z0.hi, z0.lo);
+        rz.fma2(f1.hi, f1.lo, z1.hi, z1.lo);
         if (set_p) P[li] = make_float4(z0.hi, z1.hi, z0.lo, z1.lo);
     }
 }
@@ -808,11 +859,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
     float2* const ffred = reinterpret_cast<float2*>(red);
     __shared__ float s_alpha[2], s_beta[2];
     __shared__ int s_flag;  // 0 iterate, 1 reliable update, 2 stop
-    __shared__ struct {
-        double rz, rmax2, rr64, bb, target2;
-        uint32_t k, nupd;
-        int converged;
-    } sc;  // scalar state, thread 0 only
+    __shared__ MixScalars sc;  // thread 0 only
     const unsigned G = g.g_size;
     const uint32_t rank = blockIdx.x - g.g_base;
     const uint32_t tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
@@ -822,14 +869,14 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
     const uint32_t Nn = a.A.Nn, nslot = (s1 - s0) * 32;
     const uint32_t ng = gh.count[rank];
     float4* const P = reinterpret_cast<float4*>(smem);
-    float2* const R = reinterpret_cast<float2*>(P + gh.pcap);
-    float2* const WH = R + gh.scap;
+    float2* const WH = reinterpret_cast<float2*>(P + gh.pcap);
     float2* const WL = WH + gh.scap;
     uint32_t* const GID = reinterpret_cast<uint32_t*>(WL + gh.scap);
     // slice offsets of this block, indexed by s - s0
     uint32_t* const SO = NBG_MIXED_SO_SMEM ? GID + gh.gcap
                                            : const_cast<uint32_t*>(a.A.slice_off) + s0;
     float2* __restrict__ gr = reinterpret_cast<float2*>(a.r);
+    float2* __restrict__ grl = reinterpret_cast<float2*>(a.rl);
     float2* __restrict__ xh = reinterpret_cast<float2*>(a.xh);
     float2* __restrict__ xl = reinterpret_cast<float2*>(a.xl);
     const float2* __restrict__ dinv = reinterpret_cast<const float2*>(a.A.dinv32);
@@ -838,11 +885,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
     double* const part2 = g.part + 3 * g.pstride;
     auto sync = [&]() { return grid_barrier(g.bar, G, rank, g.status); };
 
-    if (tid == 0) {
-        sc.rz = sc.rmax2 = sc.rr64 = sc.bb = sc.target2 = 0.0;
-        sc.k = sc.nupd = 0;
-        sc.converged = 0;
-    }
+    if (tid == 0) sc.clear();
     for (uint32_t j = tid; j < ng; j += kThreads) GID[j] = gh.ids[(size_t)rank * kGhostMax + j];
     if (NBG_MIXED_SO_SMEM)
         for (uint32_t j = tid; j <= s1 - s0; j += kThreads) SO[j] = a.A.slice_off[s0 + j];
@@ -855,7 +898,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         }
         double rrl = 0.0, bbl = 0.0;
         FFAcc rzk{0.f, 0.f};
-        true_residual_ghost<kThreads>(a, R, P, s0, s1, rrl, rzk, &bbl, true);
+        true_residual_ghost<kThreads>(a, P, s0, s1, rrl, rzk, &bbl, true);
         const FF t = rzk.result();
         double v[3] = {rrl, bbl, (double)t.hi + (double)t.lo};
         group_publish<3>(v, red, part2, rank);
@@ -864,20 +907,12 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
     {
         double t[3];
         group_reduce0<3>(part2, G, t);
-        if (tid == 0) {
-            sc.rr64 = t[0];
-            sc.bb = t[1];
-            sc.rz = t[2];
-            sc.target2 = (a.flags & NBG_CG_RELATIVE) ? a.tol * a.tol * sc.bb : a.tol * a.tol;
-            sc.rmax2 = sc.rr64;
-            sc.converged = !(sc.rr64 > sc.target2);
-            s_flag = (sc.converged || a.max_iter == 0) ? 2 : 0;
-        }
+        if (tid == 0) s_flag = sc.start(t, a);
         // ghosts start as their owners' p = z
         for (uint32_t j = tid; j < ng; j += kThreads) {
             const uint32_t c = GID[j];
-            const float2 rc = gr[c], dc = dinv[c];
-            const FF z0 = two_prod(rc.x, dc.x), z1 = two_prod(rc.y, dc.y);
+            const float2 rc = gr[c], rcl = grl[c], dc = dinv[c];
+            const FF z0 = ff_mulf({rc.x, rcl.x}, dc.x), z1 = ff_mulf({rc.y, rcl.y}, dc.y);
             P[nslot + j] = make_float4(z0.hi, z1.hi, z0.lo, z1.lo);
         }
         __syncthreads();
@@ -905,10 +940,10 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         }
         if (sync()) goto done;
         {
-            double pwd[1];
-            group_reduce0_ff<1>(reinterpret_cast<const float2*>(part0), G, pwd);
+            FF pw[1];
+            group_reduce0_ff<1>(reinterpret_cast<const float2*>(part0), G, pw);
             if (tid == 0) {
-                const FF al = ff_from_double(sc.rz / pwd[0]);
+                const FF al = sc.alpha(pw[0]);
                 s_alpha[0] = al.hi;
                 s_alpha[1] = al.lo;
             }
@@ -917,49 +952,59 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         {   // L2: x += alpha p, r -= alpha w, z = r / Aii; r published
             const FF alpha = {s_alpha[0], s_alpha[1]};
             FFAcc rzk{0.f, 0.f}, rrk{0.f, 0.f};
-            for (uint32_t s = s0 + warp; s < s1; s += nw) {
-                const uint32_t i = s * 32 + lane, li = i - s0 * 32;
-                if (i >= Nn) continue;
+            auto row = [&](uint32_t i, float2 xhi, float2 xlo, float2 rh, float2 rlo, float2 di) {
+                const uint32_t li = i - s0 * 32;
                 const float4 p = P[li];
                 const float2 w = WH[li], wlo = WL[li];
-                const float2 xhi = xh[i], xlo = xl[i];
-                const float2 ri = R[li], di = dinv[i];
                 const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, p.z}));
                 const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, p.w}));
                 xh[i] = make_float2(x0.hi, x1.hi);
                 xl[i] = make_float2(x0.lo, x1.lo);
                 const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
-                const FF t0 = two_sum(ri.x, -aw0.hi), t1 = two_sum(ri.y, -aw1.hi);
-                const float r0 = __fadd_rn(t0.hi, __fsub_rn(t0.lo, aw0.lo));
-                const float r1 = __fadd_rn(t1.hi, __fsub_rn(t1.lo, aw1.lo));
-                R[li] = make_float2(r0, r1);
-                gr[i] = make_float2(r0, r1);
-                const FF z0 = two_prod(r0, di.x), z1 = two_prod(r1, di.y);
-                rzk.fma2(r0, 0.f, z0.hi, z0.lo);
-                rzk.fma2(r1, 0.f, z1.hi, z1.lo);
-                rrk.fma2(r0, 0.f, r0, 0.f);
-                rrk.fma2(r1, 0.f, r1, 0.f);
+                const FF r0 = ff_add({rh.x, rlo.x}, {-aw0.hi, -aw0.lo});
+                const FF r1 = ff_add({rh.y, rlo.y}, {-aw1.hi, -aw1.lo});
+                gr[i] = make_float2(r0.hi, r1.hi);
+                grl[i] = make_float2(r0.lo, r1.lo);
+                const FF z0 = ff_mulf(r0, di.x), z1 = ff_mulf(r1, di.y);
+                rzk.fma2(r0.hi, r0.lo, z0.hi, z0.lo);
+                rzk.fma2(r1.hi, r1.lo, z1.hi, z1.lo);
+                rrk.fma2(r0.hi, r0.lo, r0.hi, r0.lo);
+                rrk.fma2(r1.hi, r1.lo, r1.hi, r1.lo);
+            };
+            // two slices per step, their global loads issued together (one
+            // memory round trip for both); rows in the same order as one
+            // slice per step, so the sums are unchanged
+            for (uint32_t s = s0 + warp; s < s1; s += 2 * nw) {
+                const uint32_t iA = s * 32 + lane, iB = iA + 32 * nw;
+                if (iA >= Nn) continue;
+                const bool vB = s + nw < s1 && iB < Nn;
+                const float2 xhA = xh[iA], xlA = xl[iA], rhA = gr[iA], rlA = grl[iA],
+                             dA = dinv[iA];
+                float2 xhB{}, xlB{}, rhB{}, rlB{}, dB{};
+                if (vB) {
+                    xhB = xh[iB];
+                    xlB = xl[iB];
+                    rhB = gr[iB];
+                    rlB = grl[iB];
+                    dB = dinv[iB];
+                }
+                row(iA, xhA, xlA, rhA, rlA, dA);
+                if (vB) row(iB, xhB, xlB, rhB, rlB, dB);
             }
             FF v[2] = {rzk.result(), rrk.result()};
             group_publish_ff<2>(v, ffred, reinterpret_cast<float2*>(part1), rank);
         }
         if (sync()) goto done;
         {
-            double t2[2];
+            FF t2[2];
             group_reduce0_ff<2>(reinterpret_cast<const float2*>(part1), G, t2);
             if (tid == 0) {
-                const double rz_new = t2[0], rr = t2[1];
-                if (rr > sc.rmax2) sc.rmax2 = rr;
-                sc.k++;
-                const int upd = rr <= a.delta * a.delta * sc.rmax2 || rr <= sc.target2 ||
-                                sc.k >= a.max_iter;
-                if (!upd) {
-                    const FF be = ff_from_double(rz_new / sc.rz);
-                    sc.rz = rz_new;
+                FF be;
+                s_flag = sc.step(t2[0], t2[1], a.max_iter, be);
+                if (!s_flag) {
                     s_beta[0] = be.hi;
                     s_beta[1] = be.lo;
                 }
-                s_flag = upd;
             }
             __syncthreads();
         }
@@ -980,7 +1025,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
             if (sync()) goto done;
             double rrl = 0.0;
             FFAcc rzk{0.f, 0.f};
-            true_residual_ghost<kThreads>(a, R, P, s0, s1, rrl, rzk, nullptr, false);
+            true_residual_ghost<kThreads>(a, P, s0, s1, rrl, rzk, nullptr, false);
             const FF t = rzk.result();
             double v[2] = {rrl, (double)t.hi + (double)t.lo};
             group_publish<2>(v, red, part2, rank);
@@ -988,18 +1033,12 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
             double tt[2];
             group_reduce0<2>(part2, G, tt);
             if (tid == 0) {
-                sc.rr64 = tt[0];
-                sc.rmax2 = sc.rr64;
-                sc.nupd++;
-                sc.converged = !(sc.rr64 > sc.target2);
-                const int stop = sc.converged || sc.k >= a.max_iter;
-                if (!stop) {
-                    const FF be = ff_from_double(tt[1] / sc.rz);
-                    sc.rz = tt[1];
+                FF be;
+                s_flag = sc.replaced(tt, a.max_iter, be);
+                if (!s_flag) {
                     s_beta[0] = be.hi;
                     s_beta[1] = be.lo;
                 }
-                s_flag = stop ? 2 : 0;
             }
             __syncthreads();
             if (s_flag == 2) break;
@@ -1007,22 +1046,35 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         {   // L3: p = z + beta p for the own rows and the ghosts (no barrier:
             // every p this block's next SpMV reads is in its shared memory)
             const FF beta = {s_beta[0], s_beta[1]};
-            for (uint32_t s = s0 + warp; s < s1; s += nw) {
-                const uint32_t i = s * 32 + lane, li = i - s0 * 32;
-                if (i >= Nn) continue;
-                const float2 ri = R[li], di = dinv[i];
-                const float4 p = P[li];
-                const FF n0 = ff_add(two_prod(ri.x, di.x), ff_mul(beta, {p.x, p.z}));
-                const FF n1 = ff_add(two_prod(ri.y, di.y), ff_mul(beta, {p.y, p.w}));
-                P[li] = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
+            // p slot l from the row's r (hi, lo) and 1/Aii
+            auto pnew = [&](uint32_t l, float2 rh, float2 rlo, float2 di) {
+                const float4 p = P[l];
+                const FF n0 = ff_add(ff_mulf({rh.x, rlo.x}, di.x), ff_mul(beta, {p.x, p.z}));
+                const FF n1 = ff_add(ff_mulf({rh.y, rlo.y}, di.y), ff_mul(beta, {p.y, p.w}));
+                P[l] = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
+            };
+            // two slices (two ghosts) per step, their loads issued together
+            for (uint32_t s = s0 + warp; s < s1; s += 2 * nw) {
+                const uint32_t iA = s * 32 + lane, iB = iA + 32 * nw;
+                if (iA >= Nn) continue;
+                const bool vB = s + nw < s1 && iB < Nn;
+                const float2 rhA = gr[iA], rlA = grl[iA], dA = dinv[iA];
+                float2 rhB{}, rlB{}, dB{};
+                if (vB) {
+                    rhB = gr[iB];
+                    rlB = grl[iB];
+                    dB = dinv[iB];
+                }
+                pnew(iA - s0 * 32, rhA, rlA, dA);
+                if (vB) pnew(iB - s0 * 32, rhB, rlB, dB);
             }
-            for (uint32_t j = tid; j < ng; j += kThreads) {
-                const uint32_t c = GID[j];
-                const float2 rc = gr[c], dc = dinv[c];
-                const float4 p = P[nslot + j];
-                const FF n0 = ff_add(two_prod(rc.x, dc.x), ff_mul(beta, {p.x, p.z}));
-                const FF n1 = ff_add(two_prod(rc.y, dc.y), ff_mul(beta, {p.y, p.w}));
-                P[nslot + j] = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
+            for (uint32_t j = tid; j < ng; j += 2 * kThreads) {
+                const uint32_t jB = j + kThreads;
+                const uint32_t cA = GID[j], cB = jB < ng ? GID[jB] : cA;
+                const float2 rhA = gr[cA], rlA = grl[cA], dA = dinv[cA];
+                const float2 rhB = gr[cB], rlB = grl[cB], dB = dinv[cB];
+                pnew(nslot + j, rhA, rlA, dA);
+                if (jB < ng) pnew(nslot + jB, rhB, rlB, dB);
             }
             __syncthreads();
         }
@@ -1077,7 +1129,7 @@ size_t ghost_plan_bytes(const nbg_bsr_t& A) {
 
 extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const float* pl,
                                   float* wh, float* wl, void* stream) {
-    if (!A || !A->b32 || !A->blo || !ph || !pl || !wh || !wl) return NBG_ERR_ARG;
+    if (!A || !A->b32 || !A->blo || !A->bxt || !ph || !pl || !wh || !wl) return NBG_ERR_ARG;
     if (sizeof(LoP::one) != 4 || sizeof(LoW::one) != 4) return NBG_ERR_ARG;  // FP32 low parts
     if (A->perm) return NBG_ERR_ARG;  // the operator alone is for layouts in mesh order
     if (A->Nn == 0) return NBG_OK;
@@ -1151,7 +1203,7 @@ int ghost_setup(const nbg_bsr_t& A, unsigned G, char* plan, cudaStream_t s, Ghos
         pcap = std::max(pcap, 32 * (s1 - s0) + cnt[b]);
         gcap = std::max(gcap, cnt[b]);
     }
-    const size_t bytes = 16 * (size_t)pcap + 24 * (size_t)scap + 4 * (size_t)gcap +
+    const size_t bytes = 16 * (size_t)pcap + 16 * (size_t)scap + 4 * (size_t)gcap +
                          (NBG_MIXED_SO_SMEM ? 4 * ((size_t)scap / 32 + 1) : 0);
     cudaFuncAttributes fa;
     if (cudaFuncGetAttributes(&fa, (const void*)k_cg_mixed_ghost) != cudaSuccess ||
@@ -1183,7 +1235,7 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     if (!result || !A) return NBG_ERR_ARG;
     *result = nbg_mixed_result_t{0, 0, 0, 0.0, 0.0};
     if (A->Nn == 0) return NBG_OK;
-    if (!A->b64 || !A->b32 || !A->blo || !A->dinv32 || !(delta > 0.0 && delta < 1.0))
+    if (!A->b64 || !A->b32 || !A->blo || !A->bxt || !A->dinv32 || !(delta > 0.0 && delta < 1.0))
         return NBG_ERR_ARG;
     cudaStream_t s = (cudaStream_t)stream;
     const size_t need = mixed_bytes(A->N), plan_bytes = ghost_plan_bytes(*A);
@@ -1210,9 +1262,10 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     a.xl = (float*)(base + 4 * f);
     a.pl = (LoP::one*)(base + 5 * f);
     a.wl = (LoW::one*)(base + 5 * f + h);
+    a.rl = (float*)(base + 5 * f + 2 * h);
     Group g;
-    g.part = (double*)(base + 5 * f + 2 * h);
-    char* tail = base + 5 * f + 2 * h + align256(kMaxBlocks * 6 * 8);
+    g.part = (double*)(base + 6 * f + 2 * h);
+    char* tail = base + 6 * f + 2 * h + align256(kMaxBlocks * 6 * 8);
     g.bar = (unsigned*)tail;
     g.status = (int*)(tail + 256);
     g.res = (double*)(tail + 512);
@@ -1263,7 +1316,7 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     g.g_base = 0;
     g.g_size = G;
     g.pstride = kMaxBlocks;
-    if (ghost) a.keep_pm = keep_permille(*A, 26.0);
+    if (ghost) a.keep_pm = keep_permille(*A, 30.0);
     g_mixed_form = ghost ? NBG_MIXED_GHOST : a.resident ? NBG_MIXED_RESIDENT_ROWS
                                                        : NBG_MIXED_GLOBAL_ROWS;
     if (e == cudaSuccess && rc == NBG_OK) {
@@ -1346,11 +1399,12 @@ void bind_vectors(MixArgs& a, char* base, uint32_t N) {
     a.xl = (float*)(base + 4 * f);
     a.pl = (LoP::one*)(base + 5 * f);
     a.wl = (LoW::one*)(base + 5 * f + h);
+    a.rl = (float*)(base + 5 * f + 2 * h);
 }
 
 double* part_slots(char* base, uint32_t N) {
     const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
-    return (double*)(base + 5 * f + 2 * h);
+    return (double*)(base + 6 * f + 2 * h);
 }
 
 // Blocks per system: one each, then one at a time to the system with the
@@ -1549,7 +1603,7 @@ extern "C" int nbg_mixed_batch_create(nbg_mixed_batch_t** out, const nbg_bsr_t* 
     if (!out || !A || A->perm) return NBG_ERR_ARG;  // instances own contiguous slices
     *out = nullptr;
     if (!A || !b || !x || !slice_ptr || n_sys == 0 || n_sys > kMaxBlocks || !A->b64 ||
-        !A->b32 || !A->blo || !A->dinv32 || !(delta > 0.0 && delta < 1.0))
+        !A->b32 || !A->blo || !A->bxt || !A->dinv32 || !(delta > 0.0 && delta < 1.0))
         return NBG_ERR_ARG;
     if (slice_ptr[0] != 0 || slice_ptr[n_sys] != A->n_slices) return NBG_ERR_ARG;
     for (uint32_t i = 0; i < n_sys; i++)

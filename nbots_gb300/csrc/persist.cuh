@@ -173,7 +173,7 @@ __device__ __forceinline__ void group_publish_ff(FF (&v)[NV], float2* scratch, f
 }
 
 // Sum over the group's blocks of NV float-float partials, in block order, by
-// warp 0 with error-free FP32 arithmetic; the result (as FP64) is valid in
+// warp 0 with error-free FP32 arithmetic; the float-float result is valid in
 // thread 0 only (no block synchronisation).
 // Lane l adds the partials of blocks l, l + 32, ... in that order; the
 // loads of kReduceBatch of them go out before the first add (one L2 round
@@ -183,7 +183,7 @@ constexpr int kReduceBatch = 5;
 
 template <int NV, int kReduceBatch = kReduceBatch>
 __device__ __forceinline__ void group_reduce0_ff(const float2* part, uint32_t G,
-                                                 double (&out)[NV]) {
+                                                 FF (&out)[NV]) {
     if (threadIdx.x < 32) {
         const uint32_t lane = threadIdx.x;
         FF v[NV];
@@ -206,7 +206,7 @@ __device__ __forceinline__ void group_reduce0_ff(const float2* part, uint32_t G,
         }
         ff_warp_sum<NV>(v);
 #pragma unroll
-        for (int k = 0; k < NV; k++) out[k] = (double)v[k].hi + (double)v[k].lo;
+        for (int k = 0; k < NV; k++) out[k] = v[k];
     }
 }
 

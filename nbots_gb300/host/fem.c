@@ -254,7 +254,7 @@ void nbg_fem_destroy(nbg_fem_t *f)
 		     f->damage,
 		     f->conn, f->row_ptr, f->col_idx, f->inc_ptr, f->inc_elem, f->distorted,
 		     f->inc_local, f->enabled, f->matched, f->status, f->cg_ws,
-		     f->slice_off, f->bcol, f->b64, f->dinv64, f->b32, f->dinv32, f->blo,
+		     f->slice_off, f->bcol, f->b64, f->dinv64, f->b32, f->dinv32, f->blo, f->bxt,
 		     f->perm, f->iperm, f->simp_rho, f->simp_out, f->simp_e, f->simp_lam};
 	for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++)
 		nbg_dev_free(p[i]);
@@ -638,11 +638,13 @@ int nbg_fem_block_layout(nbg_fem_t *f, nbg_bsr_t *out)
 		TRY(nbg_dev_alloc((void **)&f->b64, 32 * ent));
 		TRY(nbg_dev_alloc((void **)&f->b32, 16 * ent));
 		TRY(nbg_dev_alloc((void **)&f->blo, 8 * ent));
+		TRY(nbg_dev_alloc((void **)&f->bxt, 4 * ent));
 		TRY(nbg_dev_alloc((void **)&f->dinv64, 8 * (size_t)f->N));
 		TRY(nbg_dev_alloc((void **)&f->dinv32, 4 * (size_t)f->N));
 		f->bsr.b64 = f->b64;
 		f->bsr.b32 = f->b32;
 		f->bsr.blo = f->blo;
+		f->bsr.bxt = f->bxt;
 		f->bsr.dinv64 = f->dinv64;
 		f->bsr.dinv32 = f->dinv32;
 	}

@@ -30,6 +30,7 @@ struct nbg_fem {
 	double *b64, *dinv64;
 	float *b32, *dinv32;
 	uint16_t *blo;
+	uint8_t *bxt;
 	int block_order;           /* NBG_ORDER_* */
 	uint32_t block_sigma;      /* SELL-C-sigma window, 0: default */
 	uint32_t *perm, *iperm;    /* the block layout's node order, or NULL */

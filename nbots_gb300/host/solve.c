@@ -23,6 +23,7 @@ struct nbg_solver {
 	double *val, *b, *x, *b64, *dinv64;
 	float *b32, *dinv32;
 	uint16_t *blo;
+	uint8_t *bxt;
 	void *ws;
 	size_t ws_bytes;
 	nbg_bsr_t bsr;
@@ -31,7 +32,7 @@ struct nbg_solver {
 static void release(nbg_solver_t *s)
 {
 	void *p[] = {s->rp, s->ci, s->slice_off, s->bcol, s->val, s->b, s->x, s->b64,
-		     s->dinv64, s->b32, s->dinv32, s->blo, s->ws};
+		     s->dinv64, s->b32, s->dinv32, s->blo, s->bxt, s->ws};
 	for (size_t i = 0; i < sizeof(p) / sizeof(p[0]); i++)
 		nbg_dev_free(p[i]);
 	void *stream = s->stream;
@@ -91,6 +92,7 @@ int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->b64, 32 * ent);
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->b32, 16 * ent);
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->blo, 8 * ent);
+			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->bxt, 4 * ent);
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->dinv64, 8 * (size_t)N);
 			if (r2 == NBG_OK) r2 = nbg_dev_alloc((void **)&s->dinv32, 4 * (size_t)N);
 			if (r2 == NBG_OK) r2 = nbg_stream_sync(s->stream);
@@ -106,6 +108,7 @@ int nbg_solver_set_matrix(nbg_solver_t *s, uint32_t N, const uint32_t *row_ptr,
 			s->bsr.b64 = s->b64;
 			s->bsr.b32 = s->b32;
 			s->bsr.blo = s->blo;
+			s->bsr.bxt = s->bxt;
 			s->bsr.dinv64 = s->dinv64;
 			s->bsr.dinv32 = s->dinv32;
 		}
