@@ -991,8 +991,8 @@ def run_gpu(args):
             "metric": METRIC, "value": t_all, "unit": "s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": t_all * 1e3,
             "higher_is_better": False, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32 inner (float-float p, A p, x; FP32 + 16-bit remainder matrix) / f64 "
-                     "residual", "data": "synthetic",
+            "dtype": "f32 inner (float-float p, A p, x, r; FP32 + 23-bit remainder matrix) / "
+                     "f64 residual", "data": "synthetic",
             "config": {"workload": WORKLOAD, "dof": N, "nnz": nnz, "tol": TOL,
                        "l2": "flushed (512 MB write) before every timed solve",
                        "replicas": world},

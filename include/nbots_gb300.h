@@ -283,11 +283,12 @@ int nbg_cg_bsr_f64(const nbg_bsr_t *A, const double *b, double *x, uint32_t max_
                    size_t ws_bytes, void *stream);
 
 /* Mixed-precision Jacobi-PCG with reliable updates.  The Krylov iteration
- * runs entirely on the FP32 pipes: matrix b32 + blo, residual in FP32,
- * search direction, A p and the correction as FP32 pairs (float-float),
- * products and sums by error-free transformations (TwoProd / TwoSum), dot
- * products as float-float sums across threads and blocks.  Whenever the
- * FP32 residual has dropped by `delta` since the last update (and at the
+ * runs entirely on the FP32 pipes: matrix b32 + blo + bxt (about 47 bits),
+ * residual, search direction, A p and the correction as FP32 pairs
+ * (float-float), products and sums by error-free transformations (TwoProd /
+ * TwoSum), dot products as float-float sums across threads and blocks, step
+ * lengths as float-float quotients.  Whenever the recursive residual has
+ * dropped by `delta` since the last update (and at the
  * end) the correction is added to the FP64 solution x and the residual is
  * recomputed in FP64 as r = b - A x on b64.  Convergence is judged on that
  * FP64 residual. */
