@@ -218,7 +218,8 @@ int nbg_cg_f64_noalloc(uint32_t N, const uint32_t *row_ptr, const uint32_t *col_
 /* Device arrays of the node-block layout of a CSR from nb_sparse_create(.., 2)
  * (two rows per node with the same (2w, 2w+1) column pairs, sparse.c:36-52):
  * entry (slice s, k, lane r) sits at (slice_off[s] + k) * 32 + r; b64 holds
- * 4 doubles (a00 a01 a10 a11) per entry, b32 the same rounded to float, and
+ * 4 doubles (a00 a01 a10 a11) per entry, b32 the same rounded to float but
+ * column by column (a00 a10 a01 a11), and
  * the remainders (double - float) as biased 23-bit counts q + 2^22 of units
  * of 2^-46 float (|q| < 2^22): their low 16 bits in blo, their high 7 bits
  * in bxt, so that b32 + blo + bxt carries about 47 significant bits in 7

@@ -61,11 +61,14 @@ __global__ void k_bsr_fill(uint32_t Nn, const uint32_t* __restrict__ rp,
             b64[4 * e + 3] = a11;
         }
         const float h00 = (float)a00, h01 = (float)a01, h10 = (float)a10, h11 = (float)a11;
-        if (b32) reinterpret_cast<float4*>(b32)[e] = make_float4(h00, h01, h10, h11);
+        // FP32 values column by column (a00 a10 a01 a11): a column is a pair
+        // of adjacent registers for the packed FP32x2 arithmetic
+        if (b32) reinterpret_cast<float4*>(b32)[e] = make_float4(h00, h10, h01, h11);
         if (blo && bxt) {
-            // remainders (exact in FP64) as biased 23-bit counts of 2^-46 hi
-            const uint32_t q0 = rem23_encode(a00, h00), q1 = rem23_encode(a01, h01);
-            const uint32_t q2 = rem23_encode(a10, h10), q3 = rem23_encode(a11, h11);
+            // remainders (exact in FP64) as biased 23-bit counts of 2^-46 hi,
+            // in the same order
+            const uint32_t q0 = rem23_encode(a00, h00), q1 = rem23_encode(a10, h10);
+            const uint32_t q2 = rem23_encode(a01, h01), q3 = rem23_encode(a11, h11);
             uint2 packed;
             packed.x = (q0 & 0xFFFFu) | (q1 << 16);
             packed.y = (q2 & 0xFFFFu) | (q3 << 16);
@@ -128,9 +131,9 @@ __global__ void __launch_bounds__(256) k_spmv_bsr_f32(uint32_t Nn, const uint32_
         const size_t e = (size_t)k * 32 + lane;
         const float4 a = ld_hint(bv + e, pol);
         const float2 xc = xv[ld_hint(bcol + e, pol)];
-        y0 = fmaf(a.x, xc.x, y0);
-        y0 = fmaf(a.y, xc.y, y0);
-        y1 = fmaf(a.z, xc.x, y1);
+        y0 = fmaf(a.x, xc.x, y0);  // a = (a00 a10 a01 a11)
+        y0 = fmaf(a.z, xc.y, y0);
+        y1 = fmaf(a.y, xc.x, y1);
         y1 = fmaf(a.w, xc.y, y1);
     }
     reinterpret_cast<float2*>(y)[i] = make_float2(y0, y1);

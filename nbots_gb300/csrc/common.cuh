@@ -250,6 +250,30 @@ struct FFAcc {
     __device__ __forceinline__ FF result() const { return fast_two_sum(s, c); }
 };
 
+// Two accumulators of FFAcc::fma2s side by side (the two rows of a 2x2
+// block, one column at a time), on Blackwell's packed FP32x2 instructions:
+// each component takes the same roundings as FFAcc, so the sums are the
+// same bits, with half the instructions.
+struct FFAcc2 {
+    float2 s, c;
+    __device__ __forceinline__ static float2 neg(float2 v) { return make_float2(-v.x, -v.y); }
+    // (a + sc a)(x + xl) for the column a of a block, its remainder scales
+    // sc and the entry x + xl of the vector
+    __device__ __forceinline__ void fma2s(float2 a, float2 sc, float x, float xl) {
+        const float2 xx = make_float2(x, x), xxl = make_float2(xl, xl);
+        const float2 p = __fmul2_rn(a, xx);
+        float2 e = __ffma2_rn(a, xx, neg(p));
+        e = __ffma2_rn(a, xxl, e);
+        e = __ffma2_rn(sc, p, e);
+        const float2 t = __fadd2_rn(s, p);
+        const float2 bb = __fadd2_rn(t, neg(s));
+        const float2 err =
+            __fadd2_rn(__fadd2_rn(s, neg(__fadd2_rn(t, neg(bb)))), __fadd2_rn(p, neg(bb)));
+        s = t;
+        c = __fadd2_rn(c, __fadd2_rn(err, e));
+    }
+};
+
 __device__ __forceinline__ FF ff_from_double(double d) {
     const float h = (float)d;
     return {h, (float)(d - (double)h)};

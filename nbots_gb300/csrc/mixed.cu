@@ -239,7 +239,7 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     const uint32_t* __restrict__ bx = reinterpret_cast<const uint32_t*>(a.A.bxt);
     const float2* __restrict__ ph = reinterpret_cast<const float2*>(a.ph);
     const LoP::two* __restrict__ pl = reinterpret_cast<const LoP::two*>(a.pl);
-    FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
+    FFAcc2 acc{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // rows 0 and 1
     // rows past Nn in the last slice hold no entries: such lanes only
     // take part in the exchange
     const uint32_t k0 = a.A.slice_off[s] + par, k1 = live ? a.A.slice_off[s + 1] : 0;
@@ -247,16 +247,14 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     for (uint32_t k = k0; k < k1; k += 2) {
         const size_t e = (size_t)k * 32 + r;
         const uint32_t c = ld_hint(a.A.bcol + e, pol);
-        const float4 m = ld_hint(bh + e, pol);
+        const float4 m = ld_hint(bh + e, pol);  // a00 a10 a01 a11
         const float4 sc = rem23_scale4(ld_hint(bl + e, pol), ld_hint(bx + e, pol));
         const float2 pc = ph[c];
         const float2 pcl = LoP::unpack(pl[c]);
-        c0.fma2s(m.x, sc.x, pc.x, pcl.x);
-        c0.fma2s(m.y, sc.y, pc.y, pcl.y);
-        c1.fma2s(m.z, sc.z, pc.x, pcl.x);
-        c1.fma2s(m.w, sc.w, pc.y, pcl.y);
+        acc.fma2s(make_float2(m.x, m.y), make_float2(sc.x, sc.y), pc.x, pcl.x);
+        acc.fma2s(make_float2(m.z, m.w), make_float2(sc.z, sc.w), pc.y, pcl.y);
     }
-    FF t[2] = {c0.result(), c1.result()};
+    FF t[2] = {FFAcc{acc.s.x, acc.c.x}.result(), FFAcc{acc.s.y, acc.c.y}.result()};
 #pragma unroll
     for (int j = 0; j < 2; j++) {
         const float h = __shfl_xor_sync(0xffffffffu, t[j].hi, 16);
@@ -793,22 +791,20 @@ __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t
     const float4* __restrict__ bh = reinterpret_cast<const float4*>(a.A.b32);
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
     const uint32_t* __restrict__ bx = reinterpret_cast<const uint32_t*>(a.A.bxt);
-    FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
+    FFAcc2 acc{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // rows 0 and 1
     // so: this block's slice offsets, so[0] that of its first slice
     const uint32_t k0 = so[s] + par, k1 = live ? so[s + 1] : 0;
 #pragma unroll(kUnroll)
     for (uint32_t k = k0; k < k1; k += 2) {
         const size_t e = (size_t)k * 32 + r;
         const uint32_t c = ld_hint(lcol + e, pol);
-        const float4 m = ld_hint(bh + e, pol);
+        const float4 m = ld_hint(bh + e, pol);  // a00 a10 a01 a11
         const float4 sc = rem23_scale4(ld_hint(bl + e, pol), ld_hint(bx + e, pol));
         const float4 pv = P[c];
-        c0.fma2s(m.x, sc.x, pv.x, pv.z);
-        c0.fma2s(m.y, sc.y, pv.y, pv.w);
-        c1.fma2s(m.z, sc.z, pv.x, pv.z);
-        c1.fma2s(m.w, sc.w, pv.y, pv.w);
+        acc.fma2s(make_float2(m.x, m.y), make_float2(sc.x, sc.y), pv.x, pv.z);
+        acc.fma2s(make_float2(m.z, m.w), make_float2(sc.z, sc.w), pv.y, pv.w);
     }
-    FF t[2] = {c0.result(), c1.result()};
+    FF t[2] = {FFAcc{acc.s.x, acc.c.x}.result(), FFAcc{acc.s.y, acc.c.y}.result()};
 #pragma unroll
     for (int j = 0; j < 2; j++) {
         const float h = __shfl_xor_sync(0xffffffffu, t[j].hi, 16);
