@@ -338,6 +338,51 @@ __device__ __forceinline__ FF ff_mulf(FF a, float b) {
     return fast_two_sum(p.hi, __fmaf_rn(a.lo, b, p.lo));
 }
 
+// Pairs of float-float numbers (the two dofs of a node row) on the packed
+// FP32x2 instructions, each component rounded as ff_add, ff_mul and
+// ff_mulf round it.
+struct FF2 {
+    float2 hi, lo;
+};
+
+__device__ __forceinline__ float2 f2neg(float2 v) { return make_float2(-v.x, -v.y); }
+
+__device__ __forceinline__ FF2 two_sum2(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    const float2 bb = __fadd2_rn(s, f2neg(a));
+    return {s, __fadd2_rn(__fadd2_rn(a, f2neg(__fadd2_rn(s, f2neg(bb)))),
+                          __fadd2_rn(b, f2neg(bb)))};
+}
+
+__device__ __forceinline__ FF2 fast_two_sum2(float2 a, float2 b) {
+    const float2 s = __fadd2_rn(a, b);
+    return {s, __fadd2_rn(b, f2neg(__fadd2_rn(s, f2neg(a))))};
+}
+
+__device__ __forceinline__ FF2 ff2_add(FF2 a, FF2 b) {
+    const FF2 s = two_sum2(a.hi, b.hi);
+    return fast_two_sum2(s.hi, __fadd2_rn(s.lo, __fadd2_rn(a.lo, b.lo)));
+}
+
+// a * b with one float-float a for both components (a given as pairs
+// {a.hi, a.hi}, {a.lo, a.lo})
+__device__ __forceinline__ FF2 ff2_mul(FF2 a, FF2 b) {
+    const float2 p = __fmul2_rn(a.hi, b.hi);
+    float2 e = __ffma2_rn(a.hi, b.hi, f2neg(p));
+    e = __ffma2_rn(a.hi, b.lo, e);
+    e = __ffma2_rn(a.lo, b.hi, e);
+    return fast_two_sum2(p, e);
+}
+
+__device__ __forceinline__ FF2 ff2_mulf(FF2 a, float2 b) {
+    const float2 p = __fmul2_rn(a.hi, b);
+    return fast_two_sum2(p, __ffma2_rn(a.lo, b, __ffma2_rn(a.hi, b, f2neg(p))));
+}
+
+__device__ __forceinline__ FF2 ff2_bcast(FF a) {
+    return {make_float2(a.hi, a.hi), make_float2(a.lo, a.lo)};
+}
+
 // a / b, both float-float, by Dekker's long division (1971): the FP32
 // quotient q1 of the leading parts, the remainder a - q1 b in float-float,
 // and a second FP32 quotient of the remainder.  About 44 significant bits,

@@ -948,24 +948,25 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         {   // L2: x += alpha p, r -= alpha w, z = r / Aii; r published
             const FF alpha = {s_alpha[0], s_alpha[1]};
             FFAcc rzk{0.f, 0.f}, rrk{0.f, 0.f};
+            // both dofs of a row at once on the packed FP32x2 instructions
+            // (the same roundings as the global-gather form's scalar code)
+            const FF2 alpha2 = ff2_bcast(alpha);
             auto row = [&](uint32_t i, float2 xhi, float2 xlo, float2 rh, float2 rlo, float2 di) {
                 const uint32_t li = i - s0 * 32;
                 const float4 p = P[li];
-                const float2 w = WH[li], wlo = WL[li];
-                const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, p.z}));
-                const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, p.w}));
-                xh[i] = make_float2(x0.hi, x1.hi);
-                xl[i] = make_float2(x0.lo, x1.lo);
-                const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
-                const FF r0 = ff_add({rh.x, rlo.x}, {-aw0.hi, -aw0.lo});
-                const FF r1 = ff_add({rh.y, rlo.y}, {-aw1.hi, -aw1.lo});
-                gr[i] = make_float2(r0.hi, r1.hi);
-                grl[i] = make_float2(r0.lo, r1.lo);
-                const FF z0 = ff_mulf(r0, di.x), z1 = ff_mulf(r1, di.y);
-                rzk.fma2(r0.hi, r0.lo, z0.hi, z0.lo);
-                rzk.fma2(r1.hi, r1.lo, z1.hi, z1.lo);
-                rrk.fma2(r0.hi, r0.lo, r0.hi, r0.lo);
-                rrk.fma2(r1.hi, r1.lo, r1.hi, r1.lo);
+                const FF2 x = ff2_add({xhi, xlo},
+                                      ff2_mul(alpha2, {make_float2(p.x, p.y), make_float2(p.z, p.w)}));
+                xh[i] = x.hi;
+                xl[i] = x.lo;
+                const FF2 aw = ff2_mul(alpha2, {WH[li], WL[li]});
+                const FF2 r = ff2_add({rh, rlo}, {f2neg(aw.hi), f2neg(aw.lo)});
+                gr[i] = r.hi;
+                grl[i] = r.lo;
+                const FF2 z = ff2_mulf(r, di);
+                rzk.fma2(r.hi.x, r.lo.x, z.hi.x, z.lo.x);
+                rzk.fma2(r.hi.y, r.lo.y, z.hi.y, z.lo.y);
+                rrk.fma2(r.hi.x, r.lo.x, r.hi.x, r.lo.x);
+                rrk.fma2(r.hi.y, r.lo.y, r.hi.y, r.lo.y);
             };
             // two slices per step, their global loads issued together (one
             // memory round trip for both); rows in the same order as one
@@ -1043,11 +1044,12 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
             // every p this block's next SpMV reads is in its shared memory)
             const FF beta = {s_beta[0], s_beta[1]};
             // p slot l from the row's r (hi, lo) and 1/Aii
+            const FF2 beta2 = ff2_bcast(beta);
             auto pnew = [&](uint32_t l, float2 rh, float2 rlo, float2 di) {
                 const float4 p = P[l];
-                const FF n0 = ff_add(ff_mulf({rh.x, rlo.x}, di.x), ff_mul(beta, {p.x, p.z}));
-                const FF n1 = ff_add(ff_mulf({rh.y, rlo.y}, di.y), ff_mul(beta, {p.y, p.w}));
-                P[l] = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
+                const FF2 n = ff2_add(ff2_mulf({rh, rlo}, di),
+                                      ff2_mul(beta2, {make_float2(p.x, p.y), make_float2(p.z, p.w)}));
+                P[l] = make_float4(n.hi.x, n.hi.y, n.lo.x, n.lo.y);
             };
             // two slices (two ghosts) per step, their loads issued together
             for (uint32_t s = s0 + warp; s < s1; s += 2 * nw) {
