@@ -491,9 +491,9 @@ int nbg_fem_block_layout(nbg_fem_t *f, nbg_bsr_t *out);
  * SIGMA sorts each window of `sigma` nodes (0: 512, at most 1024) by row
  * length.  AUTO is the mesh order: on the 4M-dof T3 L-shape the sigma order
  * cuts the padding from 44 % to 4 % and the FP64 CG's time per iteration by
- * 7 %, but the mixed solver's time per iteration rises by 5-8 % (its
- * gathers lose locality) and its iteration count by 10-15 % (summation
- * order), so it is taken only on request. */
+ * 7-8 %, but the mixed solver's time per iteration rises by 6-8 % at every
+ * sigma from 64 to 512 (its gathers lose locality), so it is taken only on
+ * request. */
 #define NBG_ORDER_AUTO 0
 #define NBG_ORDER_MESH 1
 #define NBG_ORDER_SIGMA 2
