@@ -51,10 +51,9 @@ using namespace nbg;
 #endif
 // FP32 low parts for both p and A p: with bfloat16 ones (32 significant
 // bits) the 4M-dof unstructured T3 case needed 26,067 iterations against
-// FP64's 22,323; with FP32 ones 22,563.
-#ifndef NBG_MIXED_PLO32
-#define NBG_MIXED_PLO32 1
-#endif
+// FP64's 22,323; with FP32 ones 22,563.  p's is always FP32 (p is stored
+// as float4 {hi, hi, lo, lo} per node row, one 16-byte gather per block);
+// A p's can be made bfloat16 for experiments.
 #ifndef NBG_MIXED_WLO32
 #define NBG_MIXED_WLO32 1
 #endif
@@ -89,9 +88,9 @@ constexpr int kUnroll = NBG_MIXED_UNROLL;
 
 namespace {
 
-// Low parts of p and of A p: bfloat16 (FP32 hi + 8 bits) or FP32 (hi + lo
-// about 48 bits), chosen separately (NBG_MIXED_PLO32, NBG_MIXED_WLO32).
-#if !NBG_MIXED_PLO32 || !NBG_MIXED_WLO32
+// Low parts of A p: bfloat16 (FP32 hi + 8 bits) or FP32 (hi + lo about 48
+// bits), NBG_MIXED_WLO32.
+#if !NBG_MIXED_WLO32
 struct LoBF {
     using one = __nv_bfloat16;
     using two = __nv_bfloat162;
@@ -111,11 +110,6 @@ struct LoF32 {
     static __device__ __forceinline__ float2 unpack(two v) { return v; }
     static __device__ __forceinline__ float round(float x) { return x; }
 };
-#if NBG_MIXED_PLO32
-using LoP = LoF32;
-#else
-using LoP = LoBF;
-#endif
 #if NBG_MIXED_WLO32
 using LoW = LoF32;
 #else
@@ -127,16 +121,17 @@ using LoW = LoBF;
 #define NBG_MIXED_DV_SHARED 0
 #endif
 constexpr bool kDvShared = NBG_MIXED_DV_SHARED;
-// own-row bytes per node: x (hi, lo), r (hi, lo), A p hi, p hi (8 B each),
-// 1/Aii (8 B, when shared) and the low pairs
-constexpr size_t kOwnNodeBytes = 48 + (kDvShared ? 8 : 0) + sizeof(LoP::two) + sizeof(LoW::two);
+// own-row bytes per node: p (16 B), x (hi, lo), r (hi, lo), A p hi (8 B
+// each), 1/Aii (8 B, when shared) and A p's low pair
+constexpr size_t kOwnNodeBytes = 56 + (kDvShared ? 8 : 0) + sizeof(LoW::two);
 
 struct MixArgs {
     nbg_bsr_t A;
     const double* b;
     double* u;
-    float* ph;               // search direction, global (gathered by neighbours)
-    LoP::one* pl;
+    float4* p;                // search direction {hi, hi, lo, lo} per node row, global
+                              // (gathered by neighbours)
+    const float *ph, *pl;     // the standalone operator's input, hi and lo apart
     float *r, *wh, *xh, *xl;  // own-row vectors when they do not fit in shared memory
     float* rl;                // low part of r (float-float residual)
     LoW::one* wl;
@@ -231,6 +226,9 @@ struct MixScalars {
 // partial float-float sums are combined with one exchange; TwoSum is
 // symmetric, so both lanes hold the same bits.  Every lane of the warp must
 // call it (the exchange is warp-wide).
+// kSplit: p from the separate hi and lo arrays (the standalone operator),
+// else from the solver's interleaved copy.
+template <bool kSplit = false>
 __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, uint32_t r,
                                                 uint32_t par, bool live, uint64_t pol, FF& y0,
                                                 FF& y1) {
@@ -238,8 +236,12 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
     const uint2* __restrict__ bl = reinterpret_cast<const uint2*>(a.A.blo);
     const uint32_t* __restrict__ bx = reinterpret_cast<const uint32_t*>(a.A.bxt);
     const float2* __restrict__ ph = reinterpret_cast<const float2*>(a.ph);
-    const LoP::two* __restrict__ pl = reinterpret_cast<const LoP::two*>(a.pl);
-    FFAcc2 acc{make_float2(0.f, 0.f), make_float2(0.f, 0.f)};  // rows 0 and 1
+    const float2* __restrict__ pl = reinterpret_cast<const float2*>(a.pl);
+    const float4* __restrict__ p4 = a.p;
+    // scalar accumulators: with p gathered from global memory the packed
+    // FP32x2 form of spmv_half_local measured 5 % slower here (4M-dof T3:
+    // 192 against 183 us per iteration); the roundings are the same
+    FFAcc c0{0.f, 0.f}, c1{0.f, 0.f};
     // rows past Nn in the last slice hold no entries: such lanes only
     // take part in the exchange
     const uint32_t k0 = a.A.slice_off[s] + par, k1 = live ? a.A.slice_off[s + 1] : 0;
@@ -249,12 +251,19 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
         const uint32_t c = ld_hint(a.A.bcol + e, pol);
         const float4 m = ld_hint(bh + e, pol);  // a00 a10 a01 a11
         const float4 sc = rem23_scale4(ld_hint(bl + e, pol), ld_hint(bx + e, pol));
-        const float2 pc = ph[c];
-        const float2 pcl = LoP::unpack(pl[c]);
-        acc.fma2s(make_float2(m.x, m.y), make_float2(sc.x, sc.y), pc.x, pcl.x);
-        acc.fma2s(make_float2(m.z, m.w), make_float2(sc.z, sc.w), pc.y, pcl.y);
+        float4 pv;
+        if (kSplit) {
+            const float2 h = ph[c], l = pl[c];
+            pv = make_float4(h.x, h.y, l.x, l.y);
+        } else {
+            pv = p4[c];
+        }
+        c0.fma2s(m.x, sc.x, pv.x, pv.z);
+        c0.fma2s(m.z, sc.z, pv.y, pv.w);
+        c1.fma2s(m.y, sc.y, pv.x, pv.z);
+        c1.fma2s(m.w, sc.w, pv.y, pv.w);
     }
-    FF t[2] = {FFAcc{acc.s.x, acc.c.x}.result(), FFAcc{acc.s.y, acc.c.y}.result()};
+    FF t[2] = {c0.result(), c1.result()};
 #pragma unroll
     for (int j = 0; j < 2; j++) {
         const float h = __shfl_xor_sync(0xffffffffu, t[j].hi, 16);
@@ -268,9 +277,9 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
 // Own-row vectors of this block, indexed by local node row
 // (i - 32 * s0): shared memory when they fit, else the global workspace.
 struct Own {
-    float2 *xh, *xl, *r, *rl, *dv, *wh, *ph;
+    float4* p;  // {hi, hi, lo, lo}
+    float2 *xh, *xl, *r, *rl, *dv, *wh;
     LoW::two* wl;
-    LoP::two* pl;
 };
 
 template <bool kRes>
@@ -279,14 +288,14 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
     Own o;
     const size_t base = (size_t)s0 * 32;
     if (kRes) {
-        float2* f = reinterpret_cast<float2*>(smem);
+        o.p = reinterpret_cast<float4*>(smem);
+        float2* f = reinterpret_cast<float2*>(o.p + nrows);
         o.xh = f;
         o.xl = f + nrows;
         o.r = f + 2 * nrows;
         o.wh = f + 3 * nrows;
-        o.ph = f + 4 * nrows;
-        o.rl = f + 5 * nrows;
-        f += 6 * nrows;
+        o.rl = f + 4 * nrows;
+        f += 5 * nrows;
         if (kDvShared) {
             o.dv = f;
             f += nrows;
@@ -294,17 +303,15 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
             o.dv = const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) + base;
         }
         o.wl = reinterpret_cast<LoW::two*>(f);
-        o.pl = reinterpret_cast<LoP::two*>(o.wl + nrows);
     } else {
+        o.p = a.p + base;
         o.xh = reinterpret_cast<float2*>(a.xh) + base;
         o.xl = reinterpret_cast<float2*>(a.xl) + base;
         o.r = reinterpret_cast<float2*>(a.r) + base;
         o.rl = reinterpret_cast<float2*>(a.rl) + base;
         o.dv = const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) + base;
         o.wh = reinterpret_cast<float2*>(a.wh) + base;
-        o.ph = reinterpret_cast<float2*>(a.ph) + base;
         o.wl = reinterpret_cast<LoW::two*>(a.wl) + base;
-        o.pl = reinterpret_cast<LoP::two*>(a.pl) + base;
     }
     return o;
 }
@@ -336,12 +343,9 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
         rz.fma2(f0.hi, f0.lo, z0.hi, z0.lo);
         rz.fma2(f1.hi, f1.lo, z1.hi, z1.lo);
         if (set_p) {
-            const float2 hi = make_float2(z0.hi, z1.hi);
-            const LoP::two lo = LoP::pack(z0.lo, z1.lo);
-            o.ph[li] = hi;
-            o.pl[li] = lo;
-            reinterpret_cast<float2*>(a.ph)[i] = hi;
-            reinterpret_cast<LoP::two*>(a.pl)[i] = lo;
+            const float4 p = make_float4(z0.hi, z1.hi, z0.lo, z1.lo);
+            o.p[li] = p;
+            a.p[i] = p;  // the same slot when the own rows are in global memory
         }
     }
 }
@@ -368,8 +372,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     group_slice_range(g.s_begin, g.s_end, rank, G, s0, s1);
     const uint32_t Nn = a.A.Nn;
     const Own o = own_vectors<kRes>(a, smem, s0, (s1 - s0) * 32);
-    float2* __restrict__ gph = reinterpret_cast<float2*>(a.ph);
-    LoP::two* __restrict__ gpl = reinterpret_cast<LoP::two*>(a.pl);
+    float4* __restrict__ gp = a.p;
     double* const part0 = g.part;
     double* const part1 = g.part + g.pstride;
     double* const part2 = g.part + 3 * g.pstride;
@@ -418,10 +421,9 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
                 const float l0 = LoW::round(y0.lo), l1 = LoW::round(y1.lo);
                 o.wh[li] = make_float2(y0.hi, y1.hi);
                 o.wl[li] = LoW::pack(l0, l1);
-                const float2 p = o.ph[li];
-                const float2 plo = LoP::unpack(o.pl[li]);
-                pw.fma2(p.x, plo.x, y0.hi, l0);
-                pw.fma2(p.y, plo.y, y1.hi, l1);
+                const float4 p = o.p[li];
+                pw.fma2(p.x, p.z, y0.hi, l0);
+                pw.fma2(p.y, p.w, y1.hi, l1);
             }
             FF v[1] = {pw.result()};
             group_publish_ff<1>(v, ffred, reinterpret_cast<float2*>(part0), rank);
@@ -443,12 +445,12 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
-                const float2 p = o.ph[li], plo = LoP::unpack(o.pl[li]);
+                const float4 p = o.p[li];
                 const float2 w = o.wh[li], wlo = LoW::unpack(o.wl[li]);
                 const float2 xhi = o.xh[li], xlo = o.xl[li];
                 const float2 ri = o.r[li], rli = o.rl[li], di = o.dv[li];
-                const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, plo.x}));
-                const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, plo.y}));
+                const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, p.z}));
+                const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, p.w}));
                 o.xh[li] = make_float2(x0.hi, x1.hi);
                 o.xl[li] = make_float2(x0.lo, x1.lo);
                 const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
@@ -520,17 +522,12 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
                 const float2 ri = o.r[li], rli = o.rl[li], di = o.dv[li];
-                const float2 p = o.ph[li], plo = LoP::unpack(o.pl[li]);
-                const FF n0 = ff_add(ff_mulf({ri.x, rli.x}, di.x), ff_mul(beta, {p.x, plo.x}));
-                const FF n1 = ff_add(ff_mulf({ri.y, rli.y}, di.y), ff_mul(beta, {p.y, plo.y}));
-                const float2 hi = make_float2(n0.hi, n1.hi);
-                const LoP::two lo = LoP::pack(n0.lo, n1.lo);
-                if (kRes) {
-                    o.ph[li] = hi;
-                    o.pl[li] = lo;
-                }
-                gph[i] = hi;
-                gpl[i] = lo;
+                const float4 p = o.p[li];
+                const FF n0 = ff_add(ff_mulf({ri.x, rli.x}, di.x), ff_mul(beta, {p.x, p.z}));
+                const FF n1 = ff_add(ff_mulf({ri.y, rli.y}, di.y), ff_mul(beta, {p.y, p.w}));
+                const float4 pn = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
+                if (kRes) o.p[li] = pn;
+                gp[i] = pn;
             }
         }
         if (sync()) goto done;
@@ -606,6 +603,20 @@ size_t mixed_core_bytes(uint32_t N) {
     return 6 * f + 2 * h + align256(kMaxBlocks * 6 * 8) + 3 * 256;
 }
 
+// The vector slots at the start of a workspace (indexed by node row): r,
+// p (float4, two slots), A p hi, x hi, x lo, A p lo, r lo.
+void carve_vectors(MixArgs& a, char* base, uint32_t N) {
+    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
+    a.r = (float*)base;
+    a.p = (float4*)(base + f);
+    a.wh = (float*)(base + 3 * f);
+    a.xh = (float*)(base + 4 * f);
+    a.xl = (float*)(base + 5 * f);
+    a.wl = (LoW::one*)(base + 6 * f);
+    a.rl = (float*)(base + 6 * f + h);
+    a.ph = a.pl = nullptr;
+}
+
 // plus the permuted copies of b and x for a layout with a node order
 size_t mixed_bytes(uint32_t N) { return mixed_core_bytes(N) + perm_tail_bytes(N); }
 
@@ -625,7 +636,7 @@ __global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
         if (s * 32 + ((h & 1) << 4) >= a.A.Nn) continue;
         FF y0, y1;
         const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
-        spmv_half_split(a, s, r, par, i < a.A.Nn, pol, y0, y1);
+        spmv_half_split<true>(a, s, r, par, i < a.A.Nn, pol, y0, y1);
         if (par || i >= a.A.Nn) continue;
         wh[i] = make_float2(y0.hi, y1.hi);
         wl[i] = LoW::pack(LoW::round(y0.lo), LoW::round(y1.lo));
@@ -1128,14 +1139,14 @@ size_t ghost_plan_bytes(const nbg_bsr_t& A) {
 extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const float* pl,
                                   float* wh, float* wl, void* stream) {
     if (!A || !A->b32 || !A->blo || !A->bxt || !ph || !pl || !wh || !wl) return NBG_ERR_ARG;
-    if (sizeof(LoP::one) != 4 || sizeof(LoW::one) != 4) return NBG_ERR_ARG;  // FP32 low parts
+    if (sizeof(LoW::one) != 4) return NBG_ERR_ARG;  // FP32 low parts
     if (A->perm) return NBG_ERR_ARG;  // the operator alone is for layouts in mesh order
     if (A->Nn == 0) return NBG_OK;
     MixArgs a;
     memset(&a, 0, sizeof(a));
     a.A = *A;
-    a.ph = const_cast<float*>(ph);
-    a.pl = reinterpret_cast<LoP::one*>(const_cast<float*>(pl));
+    a.ph = ph;
+    a.pl = pl;
     a.keep_pm = keep_permille(*A);
     unsigned G = 0;
     const int rc = coop_grid((const void*)k_spmv_mixed, A->n_slices, &G, kMixThreads);
@@ -1167,7 +1178,7 @@ namespace {
 // form).  plan: the workspace region of ghost_plan_bytes(A).
 int ghost_setup(const nbg_bsr_t& A, unsigned G, char* plan, cudaStream_t s, GhostArgs* gh,
                 size_t* dyn) {
-    if (!NBG_MIXED_RESIDENT || sizeof(LoP::one) != 4 || sizeof(LoW::one) != 4) return 0;
+    if (!NBG_MIXED_RESIDENT || sizeof(LoW::one) != 4) return 0;
     uint16_t* lcol = (uint16_t*)plan;
     uint32_t* ids = (uint32_t*)(plan + align256(2 * (size_t)A.n_entries));
     uint32_t* count = ids + (size_t)G * kGhostMax;
@@ -1253,14 +1264,7 @@ extern "C" int nbg_cg_mixed(const nbg_bsr_t* A, const double* b, double* x, uint
     a.A = *A;
     a.b = b;
     a.u = x;
-    a.r = (float*)base;
-    a.ph = (float*)(base + f);
-    a.wh = (float*)(base + 2 * f);
-    a.xh = (float*)(base + 3 * f);
-    a.xl = (float*)(base + 4 * f);
-    a.pl = (LoP::one*)(base + 5 * f);
-    a.wl = (LoW::one*)(base + 5 * f + h);
-    a.rl = (float*)(base + 5 * f + 2 * h);
+    carve_vectors(a, base, A->N);
     Group g;
     g.part = (double*)(base + 6 * f + 2 * h);
     char* tail = base + 6 * f + 2 * h + align256(kMaxBlocks * 6 * 8);
@@ -1388,17 +1392,7 @@ size_t batch_bytes(uint32_t N, uint32_t n_sys) {
 
 // Vector slots of the workspace shared by every system (indexed by the
 // global node row).
-void bind_vectors(MixArgs& a, char* base, uint32_t N) {
-    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
-    a.r = (float*)base;
-    a.ph = (float*)(base + f);
-    a.wh = (float*)(base + 2 * f);
-    a.xh = (float*)(base + 3 * f);
-    a.xl = (float*)(base + 4 * f);
-    a.pl = (LoP::one*)(base + 5 * f);
-    a.wl = (LoW::one*)(base + 5 * f + h);
-    a.rl = (float*)(base + 5 * f + 2 * h);
-}
+void bind_vectors(MixArgs& a, char* base, uint32_t N) { carve_vectors(a, base, N); }
 
 double* part_slots(char* base, uint32_t N) {
     const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
