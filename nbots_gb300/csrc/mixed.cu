@@ -83,7 +83,10 @@ constexpr int kBatThreads = NBG_BATCH_THREADS;
 constexpr int kBatMinBlocks = NBG_BATCH_MIN_BLOCKS;
 constexpr int kUnroll = NBG_MIXED_UNROLL;
 #ifndef NBG_L2_KEEP
-#define NBG_L2_KEEP 50  // percent of L2 for the matrix part kept between iterations
+// percent of L2 for the matrix part kept between iterations (1M-dof ghost
+// form: 0.2500 s at 40, 0.2560 at 50, 0.2644 at 60, 0.251-0.253 at 10-30:
+// the rest of L2 holds the vectors)
+#define NBG_L2_KEEP 40
 #endif
 
 namespace {
@@ -826,9 +829,16 @@ __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t
     y1 = t[1];
 }
 
-// true_residual for the ghost form: r (float-float) to global memory, its
-// hi and lo arrays, where the owner keeps it and the blocks that hold this
-// row as a ghost read it.
+// The ghost form keeps r and x in global memory as float4 {hi of both dofs,
+// lo of both} per node row (one load and one store per row), r in the
+// slots the global-gather form gives p, x in those of x hi and lo.
+__device__ __forceinline__ float4* ghost_r(const MixArgs& a) { return a.p; }
+__device__ __forceinline__ float4* ghost_x(const MixArgs& a) {
+    return reinterpret_cast<float4*>(a.xh);
+}
+
+// true_residual for the ghost form: r (float-float) to global memory, where
+// the owner keeps it and the blocks that hold this row as a ghost read it.
 template <int kThreads>
 __device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float4* P,
                                                     uint32_t s0, uint32_t s1, double& rr,
@@ -838,8 +848,7 @@ __device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float4* P,
     const double2* __restrict__ u = reinterpret_cast<const double2*>(a.u);
     const double2* __restrict__ b = reinterpret_cast<const double2*>(a.b);
     const float2* __restrict__ dinv = reinterpret_cast<const float2*>(a.A.dinv32);
-    float2* __restrict__ gr = reinterpret_cast<float2*>(a.r);
-    float2* __restrict__ grl = reinterpret_cast<float2*>(a.rl);
+    float4* __restrict__ r4 = ghost_r(a);
     for (uint32_t s = s0 + warp; s < s1; s += nw) {
         const uint32_t i = s * 32 + lane, li = i - s0 * 32;
         if (i >= a.A.Nn) continue;
@@ -849,8 +858,7 @@ __device__ __forceinline__ void true_residual_ghost(const MixArgs& a, float4* P,
         rr = fma(r0, r0, fma(r1, r1, rr));
         if (bb) *bb = fma(bi.x, bi.x, fma(bi.y, bi.y, *bb));
         const FF f0 = ff_from_double(r0), f1 = ff_from_double(r1);
-        gr[i] = make_float2(f0.hi, f1.hi);
-        grl[i] = make_float2(f0.lo, f1.lo);
+        r4[i] = make_float4(f0.hi, f1.hi, f0.lo, f1.lo);
         const float2 di = dinv[i];
         const FF z0 = ff_mulf(f0, di.x), z1 = ff_mulf(f1, di.y);
         rz.fma2(f0.hi, f0.lo, z0.hi, z0.lo);
@@ -876,16 +884,13 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
     const uint32_t Nn = a.A.Nn, nslot = (s1 - s0) * 32;
     const uint32_t ng = gh.count[rank];
     float4* const P = reinterpret_cast<float4*>(smem);
-    float2* const WH = reinterpret_cast<float2*>(P + gh.pcap);
-    float2* const WL = WH + gh.scap;
-    uint32_t* const GID = reinterpret_cast<uint32_t*>(WL + gh.scap);
+    float4* const W = P + gh.pcap;  // A p of the own rows {hi, hi, lo, lo}
+    uint32_t* const GID = reinterpret_cast<uint32_t*>(W + gh.scap);
     // slice offsets of this block, indexed by s - s0
     uint32_t* const SO = NBG_MIXED_SO_SMEM ? GID + gh.gcap
                                            : const_cast<uint32_t*>(a.A.slice_off) + s0;
-    float2* __restrict__ gr = reinterpret_cast<float2*>(a.r);
-    float2* __restrict__ grl = reinterpret_cast<float2*>(a.rl);
-    float2* __restrict__ xh = reinterpret_cast<float2*>(a.xh);
-    float2* __restrict__ xl = reinterpret_cast<float2*>(a.xl);
+    float4* __restrict__ r4 = ghost_r(a);
+    float4* __restrict__ x4 = ghost_x(a);
     const float2* __restrict__ dinv = reinterpret_cast<const float2*>(a.A.dinv32);
     double* const part0 = g.part;
     double* const part1 = g.part + g.pstride;
@@ -900,8 +905,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         for (uint32_t s = s0 + warp; s < s1; s += nw) {
             const uint32_t i = s * 32 + lane;
             if (i >= Nn) continue;
-            xh[i] = make_float2(0.f, 0.f);
-            xl[i] = make_float2(0.f, 0.f);
+            x4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         double rrl = 0.0, bbl = 0.0;
         FFAcc rzk{0.f, 0.f};
@@ -918,8 +922,9 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
         // ghosts start as their owners' p = z
         for (uint32_t j = tid; j < ng; j += kThreads) {
             const uint32_t c = GID[j];
-            const float2 rc = gr[c], rcl = grl[c], dc = dinv[c];
-            const FF z0 = ff_mulf({rc.x, rcl.x}, dc.x), z1 = ff_mulf({rc.y, rcl.y}, dc.y);
+            const float4 rc = r4[c];
+            const float2 dc = dinv[c];
+            const FF z0 = ff_mulf({rc.x, rc.z}, dc.x), z1 = ff_mulf({rc.y, rc.w}, dc.y);
             P[nslot + j] = make_float4(z0.hi, z1.hi, z0.lo, z1.lo);
         }
         __syncthreads();
@@ -936,8 +941,7 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
                 const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
                 spmv_half_local(a, gh.lcol, P, SO, s - s0, r, par, i < Nn, pol, y0, y1);
                 if (par || i >= Nn) continue;
-                WH[li] = make_float2(y0.hi, y1.hi);
-                WL[li] = make_float2(y0.lo, y1.lo);
+                W[li] = make_float4(y0.hi, y1.hi, y0.lo, y1.lo);
                 const float4 p = P[li];
                 pw.fma2(p.x, p.z, y0.hi, y0.lo);
                 pw.fma2(p.y, p.w, y1.hi, y1.lo);
@@ -962,17 +966,16 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
             // both dofs of a row at once on the packed FP32x2 instructions
             // (the same roundings as the global-gather form's scalar code)
             const FF2 alpha2 = ff2_bcast(alpha);
-            auto row = [&](uint32_t i, float2 xhi, float2 xlo, float2 rh, float2 rlo, float2 di) {
+            auto lohi = [](float4 v) -> FF2 {
+                return {make_float2(v.x, v.y), make_float2(v.z, v.w)};
+            };
+            auto row = [&](uint32_t i, float4 xo, float4 ro, float2 di) {
                 const uint32_t li = i - s0 * 32;
-                const float4 p = P[li];
-                const FF2 x = ff2_add({xhi, xlo},
-                                      ff2_mul(alpha2, {make_float2(p.x, p.y), make_float2(p.z, p.w)}));
-                xh[i] = x.hi;
-                xl[i] = x.lo;
-                const FF2 aw = ff2_mul(alpha2, {WH[li], WL[li]});
-                const FF2 r = ff2_add({rh, rlo}, {f2neg(aw.hi), f2neg(aw.lo)});
-                gr[i] = r.hi;
-                grl[i] = r.lo;
+                const FF2 x = ff2_add(lohi(xo), ff2_mul(alpha2, lohi(P[li])));
+                x4[i] = make_float4(x.hi.x, x.hi.y, x.lo.x, x.lo.y);
+                const FF2 aw = ff2_mul(alpha2, lohi(W[li]));
+                const FF2 r = ff2_add(lohi(ro), {f2neg(aw.hi), f2neg(aw.lo)});
+                r4[i] = make_float4(r.hi.x, r.hi.y, r.lo.x, r.lo.y);
                 const FF2 z = ff2_mulf(r, di);
                 rzk.fma2(r.hi.x, r.lo.x, z.hi.x, z.lo.x);
                 rzk.fma2(r.hi.y, r.lo.y, z.hi.y, z.lo.y);
@@ -986,18 +989,17 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
                 const uint32_t iA = s * 32 + lane, iB = iA + 32 * nw;
                 if (iA >= Nn) continue;
                 const bool vB = s + nw < s1 && iB < Nn;
-                const float2 xhA = xh[iA], xlA = xl[iA], rhA = gr[iA], rlA = grl[iA],
-                             dA = dinv[iA];
-                float2 xhB{}, xlB{}, rhB{}, rlB{}, dB{};
+                const float4 xA = x4[iA], rA = r4[iA];
+                const float2 dA = dinv[iA];
+                float4 xB{}, rB{};
+                float2 dB{};
                 if (vB) {
-                    xhB = xh[iB];
-                    xlB = xl[iB];
-                    rhB = gr[iB];
-                    rlB = grl[iB];
+                    xB = x4[iB];
+                    rB = r4[iB];
                     dB = dinv[iB];
                 }
-                row(iA, xhA, xlA, rhA, rlA, dA);
-                if (vB) row(iB, xhB, xlB, rhB, rlB, dB);
+                row(iA, xA, rA, dA);
+                if (vB) row(iB, xB, rB, dB);
             }
             FF v[2] = {rzk.result(), rrk.result()};
             group_publish_ff<2>(v, ffred, reinterpret_cast<float2*>(part1), rank);
@@ -1022,13 +1024,12 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane;
                 if (i >= Nn) continue;
-                const float2 xhi = xh[i], xlo = xl[i];
+                const float4 xo = x4[i];
                 double2 ui = u[i];
-                ui.x += (double)xhi.x + (double)xlo.x;
-                ui.y += (double)xhi.y + (double)xlo.y;
+                ui.x += (double)xo.x + (double)xo.z;
+                ui.y += (double)xo.y + (double)xo.w;
                 u[i] = ui;
-                xh[i] = make_float2(0.f, 0.f);
-                xl[i] = make_float2(0.f, 0.f);
+                x4[i] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             if (sync()) goto done;
             double rrl = 0.0;
@@ -1056,9 +1057,9 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
             const FF beta = {s_beta[0], s_beta[1]};
             // p slot l from the row's r (hi, lo) and 1/Aii
             const FF2 beta2 = ff2_bcast(beta);
-            auto pnew = [&](uint32_t l, float2 rh, float2 rlo, float2 di) {
+            auto pnew = [&](uint32_t l, float4 rv, float2 di) {
                 const float4 p = P[l];
-                const FF2 n = ff2_add(ff2_mulf({rh, rlo}, di),
+                const FF2 n = ff2_add(ff2_mulf({make_float2(rv.x, rv.y), make_float2(rv.z, rv.w)}, di),
                                       ff2_mul(beta2, {make_float2(p.x, p.y), make_float2(p.z, p.w)}));
                 P[l] = make_float4(n.hi.x, n.hi.y, n.lo.x, n.lo.y);
             };
@@ -1067,23 +1068,24 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
                 const uint32_t iA = s * 32 + lane, iB = iA + 32 * nw;
                 if (iA >= Nn) continue;
                 const bool vB = s + nw < s1 && iB < Nn;
-                const float2 rhA = gr[iA], rlA = grl[iA], dA = dinv[iA];
-                float2 rhB{}, rlB{}, dB{};
+                const float4 rA = r4[iA];
+                const float2 dA = dinv[iA];
+                float4 rB{};
+                float2 dB{};
                 if (vB) {
-                    rhB = gr[iB];
-                    rlB = grl[iB];
+                    rB = r4[iB];
                     dB = dinv[iB];
                 }
-                pnew(iA - s0 * 32, rhA, rlA, dA);
-                if (vB) pnew(iB - s0 * 32, rhB, rlB, dB);
+                pnew(iA - s0 * 32, rA, dA);
+                if (vB) pnew(iB - s0 * 32, rB, dB);
             }
             for (uint32_t j = tid; j < ng; j += 2 * kThreads) {
                 const uint32_t jB = j + kThreads;
                 const uint32_t cA = GID[j], cB = jB < ng ? GID[jB] : cA;
-                const float2 rhA = gr[cA], rlA = grl[cA], dA = dinv[cA];
-                const float2 rhB = gr[cB], rlB = grl[cB], dB = dinv[cB];
-                pnew(nslot + j, rhA, rlA, dA);
-                if (jB < ng) pnew(nslot + jB, rhB, rlB, dB);
+                const float4 rA = r4[cA], rB = r4[cB];
+                const float2 dA = dinv[cA], dB = dinv[cB];
+                pnew(nslot + j, rA, dA);
+                if (jB < ng) pnew(nslot + jB, rB, dB);
             }
             __syncthreads();
         }
