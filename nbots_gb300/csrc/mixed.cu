@@ -49,14 +49,11 @@ using namespace nbg;
 #ifndef NBG_MIXED_RESIDENT
 #define NBG_MIXED_RESIDENT 1
 #endif
-// FP32 low parts for both p and A p: with bfloat16 ones (32 significant
-// bits) the 4M-dof unstructured T3 case needed 26,067 iterations against
-// FP64's 22,323; with FP32 ones 22,563.  p's is always FP32 (p is stored
-// as float4 {hi, hi, lo, lo} per node row, one 16-byte gather per block);
-// A p's can be made bfloat16 for experiments.
-#ifndef NBG_MIXED_WLO32
-#define NBG_MIXED_WLO32 1
-#endif
+// The vectors p, A p, x and r are float-float, stored as float4 {hi of both
+// dofs, lo of both} per node row: one 16-byte load or store per row and
+// vector, one gather per block entry.  (With bfloat16 low parts for p and
+// A p the 4M-dof unstructured T3 case needed 26,067 iterations against
+// FP64's 22,323; with FP32 ones 22,563.)
 #ifndef NBG_MIXED_UNROLL
 #define NBG_MIXED_UNROLL 4  // entries in flight per lane in the SpMV
 #endif
@@ -91,53 +88,24 @@ constexpr int kUnroll = NBG_MIXED_UNROLL;
 
 namespace {
 
-// Low parts of A p: bfloat16 (FP32 hi + 8 bits) or FP32 (hi + lo about 48
-// bits), NBG_MIXED_WLO32.
-#if !NBG_MIXED_WLO32
-struct LoBF {
-    using one = __nv_bfloat16;
-    using two = __nv_bfloat162;
-    static __device__ __forceinline__ two pack(float a, float b) {
-        return __floats2bfloat162_rn(a, b);
-    }
-    static __device__ __forceinline__ float2 unpack(two v) { return __bfloat1622float2(v); }
-    static __device__ __forceinline__ float round(float x) {
-        return __bfloat162float(__float2bfloat16_rn(x));
-    }
-};
-#endif
-struct LoF32 {
-    using one = float;
-    using two = float2;
-    static __device__ __forceinline__ two pack(float a, float b) { return make_float2(a, b); }
-    static __device__ __forceinline__ float2 unpack(two v) { return v; }
-    static __device__ __forceinline__ float round(float x) { return x; }
-};
-#if NBG_MIXED_WLO32
-using LoW = LoF32;
-#else
-using LoW = LoBF;
-#endif
 // 1/Aii in shared memory too, or read from global memory (L2) when the
 // shared memory is better left to the L1 cache of the SpMV's gathers
 #ifndef NBG_MIXED_DV_SHARED
 #define NBG_MIXED_DV_SHARED 0
 #endif
 constexpr bool kDvShared = NBG_MIXED_DV_SHARED;
-// own-row bytes per node: p (16 B), x (hi, lo), r (hi, lo), A p hi (8 B
-// each), 1/Aii (8 B, when shared) and A p's low pair
-constexpr size_t kOwnNodeBytes = 56 + (kDvShared ? 8 : 0) + sizeof(LoW::two);
+// own-row bytes per node: p, x, r, A p (16 B each) and 1/Aii (8 B, when
+// shared)
+constexpr size_t kOwnNodeBytes = 64 + (kDvShared ? 8 : 0);
 
 struct MixArgs {
     nbg_bsr_t A;
     const double* b;
     double* u;
-    float4* p;                // search direction {hi, hi, lo, lo} per node row, global
-                              // (gathered by neighbours)
-    const float *ph, *pl;     // the standalone operator's input, hi and lo apart
-    float *r, *wh, *xh, *xl;  // own-row vectors when they do not fit in shared memory
-    float* rl;                // low part of r (float-float residual)
-    LoW::one* wl;
+    float4* p;             // search direction, global (gathered by neighbours)
+    float4 *x4, *r4, *w4;  // x, r, A p of the rows: own rows when they do not fit in
+                           // shared memory (the ghost form keeps x and r there)
+    const float *ph, *pl;  // the standalone operator's input, hi and lo apart
     uint32_t max_iter;
     double tol, delta;
     unsigned flags;
@@ -280,9 +248,8 @@ __device__ __forceinline__ void spmv_half_split(const MixArgs& a, uint32_t s, ui
 // Own-row vectors of this block, indexed by local node row
 // (i - 32 * s0): shared memory when they fit, else the global workspace.
 struct Own {
-    float4* p;  // {hi, hi, lo, lo}
-    float2 *xh, *xl, *r, *rl, *dv, *wh;
-    LoW::two* wl;
+    float4 *p, *x, *r, *w;  // {hi, hi, lo, lo}
+    float2* dv;
 };
 
 template <bool kRes>
@@ -292,29 +259,18 @@ __device__ __forceinline__ Own own_vectors(const MixArgs& a, unsigned char* smem
     const size_t base = (size_t)s0 * 32;
     if (kRes) {
         o.p = reinterpret_cast<float4*>(smem);
-        float2* f = reinterpret_cast<float2*>(o.p + nrows);
-        o.xh = f;
-        o.xl = f + nrows;
-        o.r = f + 2 * nrows;
-        o.wh = f + 3 * nrows;
-        o.rl = f + 4 * nrows;
-        f += 5 * nrows;
-        if (kDvShared) {
-            o.dv = f;
-            f += nrows;
-        } else {
-            o.dv = const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) + base;
-        }
-        o.wl = reinterpret_cast<LoW::two*>(f);
+        o.x = o.p + nrows;
+        o.r = o.p + 2 * nrows;
+        o.w = o.p + 3 * nrows;
+        o.dv = kDvShared ? reinterpret_cast<float2*>(o.p + 4 * nrows)
+                         : const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) +
+                               base;
     } else {
         o.p = a.p + base;
-        o.xh = reinterpret_cast<float2*>(a.xh) + base;
-        o.xl = reinterpret_cast<float2*>(a.xl) + base;
-        o.r = reinterpret_cast<float2*>(a.r) + base;
-        o.rl = reinterpret_cast<float2*>(a.rl) + base;
+        o.x = a.x4 + base;
+        o.r = a.r4 + base;
+        o.w = a.w4 + base;
         o.dv = const_cast<float2*>(reinterpret_cast<const float2*>(a.A.dinv32)) + base;
-        o.wh = reinterpret_cast<float2*>(a.wh) + base;
-        o.wl = reinterpret_cast<LoW::two*>(a.wl) + base;
     }
     return o;
 }
@@ -339,8 +295,7 @@ __device__ __forceinline__ void true_residual(const MixArgs& a, const Own& o, ui
         rr = fma(r0, r0, fma(r1, r1, rr));
         if (bb) *bb = fma(bi.x, bi.x, fma(bi.y, bi.y, *bb));
         const FF f0 = ff_from_double(r0), f1 = ff_from_double(r1);
-        o.r[li] = make_float2(f0.hi, f1.hi);
-        o.rl[li] = make_float2(f0.lo, f1.lo);
+        o.r[li] = make_float4(f0.hi, f1.hi, f0.lo, f1.lo);
         const float2 di = o.dv[li];
         const FF z0 = ff_mulf(f0, di.x), z1 = ff_mulf(f1, di.y);
         rz.fma2(f0.hi, f0.lo, z0.hi, z0.lo);
@@ -388,8 +343,7 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             const uint32_t i = s * 32 + lane, li = i - s0 * 32;
             if (i >= Nn) continue;
             if (kRes && kDvShared) o.dv[li] = gdv[i];
-            o.xh[li] = make_float2(0.f, 0.f);
-            o.xl[li] = make_float2(0.f, 0.f);
+            o.x[li] = make_float4(0.f, 0.f, 0.f, 0.f);
         }
         __syncwarp();
         double rrl = 0.0, bbl = 0.0;
@@ -421,12 +375,10 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
                 const uint64_t pol = l2_policy((s - s0) * 1000u < a.keep_pm * (s1 - s0));
                 spmv_half_split(a, s, r, par, i < Nn, pol, y0, y1);
                 if (par || i >= Nn) continue;
-                const float l0 = LoW::round(y0.lo), l1 = LoW::round(y1.lo);
-                o.wh[li] = make_float2(y0.hi, y1.hi);
-                o.wl[li] = LoW::pack(l0, l1);
+                o.w[li] = make_float4(y0.hi, y1.hi, y0.lo, y1.lo);
                 const float4 p = o.p[li];
-                pw.fma2(p.x, p.z, y0.hi, l0);
-                pw.fma2(p.y, p.w, y1.hi, l1);
+                pw.fma2(p.x, p.z, y0.hi, y0.lo);
+                pw.fma2(p.y, p.w, y1.hi, y1.lo);
             }
             FF v[1] = {pw.result()};
             group_publish_ff<1>(v, ffred, reinterpret_cast<float2*>(part0), rank);
@@ -448,19 +400,15 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
-                const float4 p = o.p[li];
-                const float2 w = o.wh[li], wlo = LoW::unpack(o.wl[li]);
-                const float2 xhi = o.xh[li], xlo = o.xl[li];
-                const float2 ri = o.r[li], rli = o.rl[li], di = o.dv[li];
-                const FF x0 = ff_add({xhi.x, xlo.x}, ff_mul(alpha, {p.x, p.z}));
-                const FF x1 = ff_add({xhi.y, xlo.y}, ff_mul(alpha, {p.y, p.w}));
-                o.xh[li] = make_float2(x0.hi, x1.hi);
-                o.xl[li] = make_float2(x0.lo, x1.lo);
-                const FF aw0 = ff_mul(alpha, {w.x, wlo.x}), aw1 = ff_mul(alpha, {w.y, wlo.y});
-                const FF r0 = ff_add({ri.x, rli.x}, {-aw0.hi, -aw0.lo});
-                const FF r1 = ff_add({ri.y, rli.y}, {-aw1.hi, -aw1.lo});
-                o.r[li] = make_float2(r0.hi, r1.hi);
-                o.rl[li] = make_float2(r0.lo, r1.lo);
+                const float4 p = o.p[li], w = o.w[li], xo = o.x[li], ri = o.r[li];
+                const float2 di = o.dv[li];
+                const FF x0 = ff_add({xo.x, xo.z}, ff_mul(alpha, {p.x, p.z}));
+                const FF x1 = ff_add({xo.y, xo.w}, ff_mul(alpha, {p.y, p.w}));
+                o.x[li] = make_float4(x0.hi, x1.hi, x0.lo, x1.lo);
+                const FF aw0 = ff_mul(alpha, {w.x, w.z}), aw1 = ff_mul(alpha, {w.y, w.w});
+                const FF r0 = ff_add({ri.x, ri.z}, {-aw0.hi, -aw0.lo});
+                const FF r1 = ff_add({ri.y, ri.w}, {-aw1.hi, -aw1.lo});
+                o.r[li] = make_float4(r0.hi, r1.hi, r0.lo, r1.lo);
                 const FF z0 = ff_mulf(r0, di.x), z1 = ff_mulf(r1, di.y);
                 rzk.fma2(r0.hi, r0.lo, z0.hi, z0.lo);
                 rzk.fma2(r1.hi, r1.lo, z1.hi, z1.lo);
@@ -490,13 +438,12 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
-                const float2 xhi = o.xh[li], xlo = o.xl[li];
+                const float4 xo = o.x[li];
                 double2 ui = u[i];
-                ui.x += (double)xhi.x + (double)xlo.x;
-                ui.y += (double)xhi.y + (double)xlo.y;
+                ui.x += (double)xo.x + (double)xo.z;
+                ui.y += (double)xo.y + (double)xo.w;
                 u[i] = ui;
-                o.xh[li] = make_float2(0.f, 0.f);
-                o.xl[li] = make_float2(0.f, 0.f);
+                o.x[li] = make_float4(0.f, 0.f, 0.f, 0.f);
             }
             if (sync()) goto done;
             double rrl = 0.0;
@@ -524,10 +471,10 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
             for (uint32_t s = s0 + warp; s < s1; s += nw) {
                 const uint32_t i = s * 32 + lane, li = i - s0 * 32;
                 if (i >= Nn) continue;
-                const float2 ri = o.r[li], rli = o.rl[li], di = o.dv[li];
-                const float4 p = o.p[li];
-                const FF n0 = ff_add(ff_mulf({ri.x, rli.x}, di.x), ff_mul(beta, {p.x, p.z}));
-                const FF n1 = ff_add(ff_mulf({ri.y, rli.y}, di.y), ff_mul(beta, {p.y, p.w}));
+                const float4 ri = o.r[li], p = o.p[li];
+                const float2 di = o.dv[li];
+                const FF n0 = ff_add(ff_mulf({ri.x, ri.z}, di.x), ff_mul(beta, {p.x, p.z}));
+                const FF n1 = ff_add(ff_mulf({ri.y, ri.w}, di.y), ff_mul(beta, {p.y, p.w}));
                 const float4 pn = make_float4(n0.hi, n1.hi, n0.lo, n1.lo);
                 if (kRes) o.p[li] = pn;
                 gp[i] = pn;
@@ -606,17 +553,14 @@ size_t mixed_core_bytes(uint32_t N) {
     return 6 * f + 2 * h + align256(kMaxBlocks * 6 * 8) + 3 * 256;
 }
 
-// The vector slots at the start of a workspace (indexed by node row): r,
-// p (float4, two slots), A p hi, x hi, x lo, A p lo, r lo.
+// The vector slots at the start of a workspace (indexed by node row, a
+// float4 each): p, x, r, A p.
 void carve_vectors(MixArgs& a, char* base, uint32_t N) {
-    const size_t f = align256((size_t)N * 4), h = align256((size_t)N * 4);
-    a.r = (float*)base;
-    a.p = (float4*)(base + f);
-    a.wh = (float*)(base + 3 * f);
-    a.xh = (float*)(base + 4 * f);
-    a.xl = (float*)(base + 5 * f);
-    a.wl = (LoW::one*)(base + 6 * f);
-    a.rl = (float*)(base + 6 * f + h);
+    const size_t f = align256((size_t)N * 4);
+    a.p = (float4*)base;
+    a.x4 = (float4*)(base + 2 * f);
+    a.r4 = (float4*)(base + 4 * f);
+    a.w4 = (float4*)(base + 6 * f);
     a.ph = a.pl = nullptr;
 }
 
@@ -628,7 +572,7 @@ size_t mixed_bytes(uint32_t N) { return mixed_core_bytes(N) + perm_tail_bytes(N)
 // (the first keep_pm / 1000 of each block's slices evict_last).  One block per
 // SM, slices split evenly, as in the solver.
 __global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
-    k_spmv_mixed(MixArgs a, float2* __restrict__ wh, LoW::two* __restrict__ wl) {
+    k_spmv_mixed(MixArgs a, float2* __restrict__ wh, float2* __restrict__ wl) {
     uint32_t s0, s1;
     slice_range(a.A.n_slices, s0, s1);
     const uint32_t lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
@@ -642,7 +586,7 @@ __global__ void __launch_bounds__(kMixThreads, kMixMinBlocks)
         spmv_half_split<true>(a, s, r, par, i < a.A.Nn, pol, y0, y1);
         if (par || i >= a.A.Nn) continue;
         wh[i] = make_float2(y0.hi, y1.hi);
-        wl[i] = LoW::pack(LoW::round(y0.lo), LoW::round(y1.lo));
+        wl[i] = make_float2(y0.lo, y1.lo);
     }
 }
 
@@ -829,13 +773,10 @@ __device__ __forceinline__ void spmv_half_local(const MixArgs& a, const uint16_t
     y1 = t[1];
 }
 
-// The ghost form keeps r and x in global memory as float4 {hi of both dofs,
-// lo of both} per node row (one load and one store per row), r in the
-// slots the global-gather form gives p, x in those of x hi and lo.
-__device__ __forceinline__ float4* ghost_r(const MixArgs& a) { return a.p; }
-__device__ __forceinline__ float4* ghost_x(const MixArgs& a) {
-    return reinterpret_cast<float4*>(a.xh);
-}
+// The ghost form keeps r and x in global memory (the workspace's r and x
+// rows).
+__device__ __forceinline__ float4* ghost_r(const MixArgs& a) { return a.r4; }
+__device__ __forceinline__ float4* ghost_x(const MixArgs& a) { return a.x4; }
 
 // true_residual for the ghost form: r (float-float) to global memory, where
 // the owner keeps it and the blocks that hold this row as a ghost read it.
@@ -1141,7 +1082,6 @@ size_t ghost_plan_bytes(const nbg_bsr_t& A) {
 extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const float* pl,
                                   float* wh, float* wl, void* stream) {
     if (!A || !A->b32 || !A->blo || !A->bxt || !ph || !pl || !wh || !wl) return NBG_ERR_ARG;
-    if (sizeof(LoW::one) != 4) return NBG_ERR_ARG;  // FP32 low parts
     if (A->perm) return NBG_ERR_ARG;  // the operator alone is for layouts in mesh order
     if (A->Nn == 0) return NBG_OK;
     MixArgs a;
@@ -1154,7 +1094,7 @@ extern "C" int nbg_spmv_bsr_mixed(const nbg_bsr_t* A, const float* ph, const flo
     const int rc = coop_grid((const void*)k_spmv_mixed, A->n_slices, &G, kMixThreads);
     if (rc != NBG_OK) return rc;
     k_spmv_mixed<<<G, kMixThreads, 0, (cudaStream_t)stream>>>(
-        a, reinterpret_cast<float2*>(wh), reinterpret_cast<LoW::two*>(wl));
+        a, reinterpret_cast<float2*>(wh), reinterpret_cast<float2*>(wl));
     NBG_CHECK(cudaGetLastError());
     return NBG_OK;
 }
@@ -1180,7 +1120,7 @@ namespace {
 // form).  plan: the workspace region of ghost_plan_bytes(A).
 int ghost_setup(const nbg_bsr_t& A, unsigned G, char* plan, cudaStream_t s, GhostArgs* gh,
                 size_t* dyn) {
-    if (!NBG_MIXED_RESIDENT || sizeof(LoW::one) != 4) return 0;
+    if (!NBG_MIXED_RESIDENT) return 0;
     uint16_t* lcol = (uint16_t*)plan;
     uint32_t* ids = (uint32_t*)(plan + align256(2 * (size_t)A.n_entries));
     uint32_t* count = ids + (size_t)G * kGhostMax;
