@@ -48,6 +48,10 @@ int nbg_d2h(void *dst, const void *src, size_t bytes, void *stream);
 int nbg_d2d(void *dst, const void *src, size_t bytes, void *stream);
 int nbg_memset(void *dst, int value, size_t bytes, void *stream);
 int nbg_stream_sync(void *stream);
+/* 1 when kernels on the current device read and write ordinary (pageable)
+ * host memory coherently through the host's page tables, as a Grace CPU's
+ * memory over NVLink-C2C; else 0. */
+int nbg_host_memory_access(void);
 /* Device-side bounded wait: one thread polls *flag (device memory) until it
  * equals `expect`; after limit_ns nanoseconds it stores NBG_ERR_TIMEOUT in
  * *status (device memory) and returns, leaving the context usable. */

@@ -83,6 +83,7 @@ SIGS = {
     "nbg_d2h": ([vp, vp, sz, vp], i32),
     "nbg_memset": ([vp, i32, sz, vp], i32),
     "nbg_stream_sync": ([vp], i32),
+    "nbg_host_memory_access": ([], i32),
     "nbg_wait_flag": ([vp, i32, u64, vp, vp], i32),
     "nbg_element_stiffness_f64": ([u32, u32, vp, vp, vp, f64, f64, f64, i32, f64, f64, vp, vp,
                                    vp, vp, vp], i32),

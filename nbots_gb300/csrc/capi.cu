@@ -74,6 +74,18 @@ extern "C" int nbg_stream_sync(void* stream) {
     return NBG_OK;
 }
 
+extern "C" int nbg_host_memory_access(void) {
+    int dev = 0, pageable = 0, host_tables = 0;
+    if (cudaGetDevice(&dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&pageable, cudaDevAttrPageableMemoryAccess, dev) != cudaSuccess ||
+        cudaDeviceGetAttribute(&host_tables, cudaDevAttrPageableMemoryAccessUsesHostPageTables,
+                               dev) != cudaSuccess) {
+        cudaGetLastError();
+        return 0;
+    }
+    return pageable == 1 && host_tables == 1;
+}
+
 extern "C" int nbg_host_alloc(void** ptr, size_t bytes) {
     if (!ptr) return NBG_ERR_ARG;
     *ptr = nullptr;

@@ -37,6 +37,36 @@ def test_multiply_vector_bit_exact(G, name):
     G.nb_sparse_destroy(A)
 
 
+def test_multiply_vector_both_transfer_paths():
+    """Where the GPU reaches host memory coherently (Grace, NVLink-C2C) the
+    SpMV writes the caller's y itself; NBG_HOST_DIRECT=0 keeps the copy
+    back.  Both give nbots' bits (child processes: each picks its path when
+    its first matrix is made)."""
+    import os
+    import subprocess
+    import sys
+    from conftest import ROOT
+    code = (
+        "import sys, numpy as np; sys.path.insert(0, %r); sys.path.insert(0, %r)\n"
+        "from conftest import load_golden\n"
+        "from nbots_gb300.dropin import libs, sparse_from_csr\n"
+        "G = libs()[0]\n"
+        "p, d = load_golden('c1_q4_64x32')\n"
+        "A, keep = sparse_from_csr(p, d['K_bc'])\n"
+        "y = np.zeros(p.n_dof); x = np.ascontiguousarray(d['spmv_x'])\n"
+        "for _ in range(3):\n"
+        "    G.nb_sparse_multiply_vector(A, x.ctypes.data, y.ctypes.data, 1)\n"
+        "    assert np.array_equal(y.view(np.uint64), d['spmv_y'].view(np.uint64))\n"
+        "assert G.nbg_dropin_error() == 0\n"
+        "print('OK')\n" % (ROOT, os.path.join(ROOT, "tests")))
+    for direct in ("0", "1"):
+        env = dict(os.environ, NBG_HOST_DIRECT=direct)
+        env.pop("NBG_DROPIN_CPU", None)
+        r = subprocess.run([sys.executable, "-c", code], capture_output=True, text=True,
+                           env=env, timeout=300)
+        assert r.returncode == 0 and r.stdout.strip().endswith("OK"), r.stdout + r.stderr
+
+
 @pytest.mark.parametrize("name", [c for c in GOLDEN_CASES if c != "q4_distorted_8x4"])
 def test_cg_precond_jacobi(G, name):
     from nbots_gb300.dropin import sparse_from_csr
