@@ -160,6 +160,41 @@ __device__ __forceinline__ int grid_barrier(unsigned* bar, unsigned nblocks, uns
     return barrier_wait(bar, old, status);
 }
 
+// Counting form of the same barrier: every block adds 1 per barrier with a
+// release reduction that returns nothing (no round trip before the first
+// poll) and waits, with acquire loads, until the word reaches nblocks times
+// the number of barriers it has passed, which each thread keeps in
+// `target` (zero at the start; every block of the group passes the same
+// barriers).  The word is zero at launch.  Bounded as barrier_wait.
+__device__ __forceinline__ int grid_barrier_count(unsigned* bar, unsigned nblocks,
+                                                  unsigned& target, int* status) {
+    __shared__ int s_stop;
+    __syncthreads();
+    target += nblocks;
+    if (threadIdx.x == 0) {
+        asm volatile("red.release.gpu.global.add.u32 [%0], %1;" ::"l"(bar), "r"(1u) : "memory");
+        int stop = 0;
+        uint64_t t0 = 0;
+        for (unsigned it = 0;; it++) {
+            if ((int)(ld_acquire(bar) - target) >= 0) break;
+            if ((it & 63u) == 0) {
+                const uint64_t t = globaltimer();
+                if (it == 0) {
+                    t0 = t;
+                } else if (t - t0 > kSpinLimitNs) {
+                    atomicCAS(status, 0, NBG_ERR_TIMEOUT);
+                    stop = 1;
+                    break;
+                }
+            }
+        }
+        if (!stop && ld_volatile(status) != 0) stop = 1;
+        s_stop = stop;
+    }
+    __syncthreads();
+    return s_stop;
+}
+
 // Block-wide sum of NV values per thread, fixed tree order.  Result valid in
 // thread 0.  `scratch` holds NV * 32 doubles.
 template <int NV>

@@ -79,6 +79,13 @@ constexpr int kMixMinBlocks = NBG_MIXED_MIN_BLOCKS;
 constexpr int kBatThreads = NBG_BATCH_THREADS;
 constexpr int kBatMinBlocks = NBG_BATCH_MIN_BLOCKS;
 constexpr int kUnroll = NBG_MIXED_UNROLL;
+// The ghost-node form's grid barriers by counting (grid_barrier_count),
+// whose arrival is a reduction with no return value: 0.2422 against 0.2443
+// s per 1M-dof solve with the arrival that returns the old word
+// (grid_barrier).
+#ifndef NBG_BARRIER_COUNT
+#define NBG_BARRIER_COUNT 1
+#endif
 #ifndef NBG_L2_KEEP
 // percent of L2 for the matrix part kept between iterations (1M-dof ghost
 // form: 0.2500 s at 40, 0.2560 at 50, 0.2644 at 60, 0.251-0.253 at 10-30:
@@ -334,6 +341,9 @@ __device__ __forceinline__ void mixed_solve(const MixArgs& a, const Group& g, un
     double* const part0 = g.part;
     double* const part1 = g.part + g.pstride;
     double* const part2 = g.part + 3 * g.pstride;
+    // the arrival that returns the old word: with the counting barrier the
+    // global-gather and batched launches ran slower (4M-dof T3: 4.19 against
+    // 4.07 s; the 96-system batch: 1.43 against 1.36 s)
     auto sync = [&]() { return grid_barrier(g.bar, G, rank, g.status); };
 
     if (threadIdx.x == 0) sc.clear();
@@ -836,7 +846,12 @@ __device__ __forceinline__ void mixed_solve_ghost(const MixArgs& a, const Group&
     double* const part0 = g.part;
     double* const part1 = g.part + g.pstride;
     double* const part2 = g.part + 3 * g.pstride;
+#if NBG_BARRIER_COUNT
+    unsigned bar_target = 0;
+    auto sync = [&]() { return grid_barrier_count(g.bar, G, bar_target, g.status); };
+#else
     auto sync = [&]() { return grid_barrier(g.bar, G, rank, g.status); };
+#endif
 
     if (tid == 0) sc.clear();
     for (uint32_t j = tid; j < ng; j += kThreads) GID[j] = gh.ids[(size_t)rank * kGhostMax + j];
